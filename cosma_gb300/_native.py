@@ -1,0 +1,98 @@
+"""ctypes bindings of the C ABI declared in include/cosma_gb300.h.
+
+The shared library is built in-tree (cosma_gb300/_lib/libcosma_gb300.so).
+There is no fallback: if the library is missing or fails to load, every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libcosma_gb300.so"
+
+SUCCESS = 0
+METHOD_AUTO, METHOD_NATIVE, METHOD_OZAKI, METHOD_BF16X3 = 0, 1, 2, 3
+METHODS = {"auto": METHOD_AUTO, "native": METHOD_NATIVE, "ozaki": METHOD_OZAKI, "bf16x3": METHOD_BF16X3}
+
+
+class CosmaGpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"cosma_gb300 error {code}: {message}")
+        self.code = code
+
+
+class OzakiInfo(C.Structure):
+    _fields_ = [("slices", C.c_int), ("products", C.c_int), ("groups", C.c_int), ("fallback_native", C.c_int),
+                ("spread_bits", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+i32, i64, dbl, flt, vp, ch = C.c_int, C.c_int64, C.c_double, C.c_float, C.c_void_p, C.c_char
+_PX = [vp] * 19
+
+SIGNATURES = {
+    "cosma_gpu_last_error": (i32, []),
+    "cosma_gpu_last_error_string": (C.c_char_p, []),
+    "cosma_gpu_version": (C.c_char_p, []),
+    "cosma_gpu_tmm_make_context": (vp, [ch, i32, i32, i32, i32]),
+    "cosma_gpu_tmm_destroy_context": (None, [vp]),
+    "cosma_gpu_tmm_set_method": (i32, [vp, i32, i32]),
+    "cosma_gpu_tmm_device_buffer_c": (vp, [vp]),
+    "cosma_gpu_tmm_last_ozaki_info": (i32, [vp, C.POINTER(OzakiInfo)]),
+    "cosma_gpu_tmm_gemm_s": (i32, [vp, ch, ch, i32, i32, i32, flt, vp, i32, vp, i32, flt, vp, i32, i32, i32]),
+    "cosma_gpu_tmm_gemm_d": (i32, [vp, ch, ch, i32, i32, i32, dbl, vp, i32, vp, i32, dbl, vp, i32, i32, i32]),
+    "cosma_gpu_tmm_gemm_c": (i32, [vp, ch, ch, i32, i32, i32, vp, vp, i32, vp, i32, vp, vp, i32, i32, i32]),
+    "cosma_gpu_tmm_gemm_z": (i32, [vp, ch, ch, i32, i32, i32, vp, vp, i32, vp, i32, vp, vp, i32, i32, i32]),
+    "cosma_gpu_local_multiply_s": (i32, [vp, vp, vp, vp, i32, i32, i32, flt, flt, i32]),
+    "cosma_gpu_local_multiply_d": (i32, [vp, vp, vp, vp, i32, i32, i32, dbl, dbl, i32]),
+    "cosma_gpu_local_multiply_c": (i32, [vp, vp, vp, vp, i32, i32, i32, vp, vp, i32]),
+    "cosma_gpu_local_multiply_z": (i32, [vp, vp, vp, vp, i32, i32, i32, vp, vp, i32]),
+    "cosma_gpu_context_instance": (vp, [ch]),
+    "cosma_gpu_dgemm_device": (i32, [i32, ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, vp]),
+    "cosma_gpu_zgemm_device": (i32, [i32, ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
+    "cosma_gpu_sgemm_device": (i32, [i32, ch, ch, i64, i64, i64, flt, vp, i64, vp, i64, flt, vp, i64, vp]),
+    "cosma_gpu_cgemm_device": (i32, [i32, ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
+    "cosma_gpu_dgemm_ozaki_device": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
+                                           C.POINTER(OzakiInfo)]),
+    "costa_gpu_pack": (i32, [ch, i32, i32, i64, i64, vp, i64, vp, i64, vp]),
+    "costa_gpu_unpack_d": (i32, [i64, i64, dbl, vp, i64, dbl, vp, i64, vp]),
+    "costa_gpu_unpack_s": (i32, [i64, i64, flt, vp, i64, flt, vp, i64, vp]),
+    "costa_gpu_unpack_z": (i32, [i64, i64, vp, vp, i64, vp, vp, i64, vp]),
+    "costa_gpu_unpack_c": (i32, [i64, i64, vp, vp, i64, vp, vp, i64, vp]),
+    "cosma_gpu_pxgemm_set_method": (i32, [i32]),
+}
+for _pre in ("p", "P", "cosma_p", "COSMA_P"):
+    for _t in "sdcz":
+        t = _t if _pre[-1] == "p" else _t.upper()
+        for _suf in ("", "_"):
+            base = f"{_pre}{t}gemm" if _pre[-1] == "p" else f"{_pre}{t}GEMM"
+            SIGNATURES[base + _suf] = (None, _PX)
+
+_lib = None
+
+
+def load():
+    """Loads the library (building nothing); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m cosma_gb300.build` "
+                          "(there is no non-CUDA fallback)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int):
+    if status != SUCCESS:
+        lib = load()
+        raise CosmaGpuError(status, lib.cosma_gpu_last_error_string().decode(errors="replace"))
+    return status

@@ -1,0 +1,221 @@
+"""Python mirror of the reference interfaces for the one-rank GEMM path.
+
+Names, argument order and meaning follow the reference:
+  * ``make_context`` / ``gemm``      -> Tiled-MM ``gpu::make_context`` / ``gpu::gemm``
+    (call sites src/cosma/context.cpp:24-25, src/cosma/local_multiply.cpp:245-260)
+  * ``local_multiply``               -> ``cosma::local_multiply`` (src/cosma/local_multiply.hpp:6-49)
+  * ``pxgemm``                       -> ``cosma::pxgemm`` / ``p?gemm_`` (src/cosma/cosma_pxgemm.cpp:16-34)
+Matrices are column-major buffers: numpy arrays (host) or torch tensors
+(host or CUDA).  A 2-D torch tensor is taken in column-major form when
+``stride(0) == 1``; any buffer may also be passed flat with explicit sizes
+and leading dimensions, exactly as through the C ABI.  Every call goes
+through the CUDA library; failures raise ``CosmaGpuError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+_DT = {"s": np.float32, "d": np.float64, "c": np.complex64, "z": np.complex128}
+
+
+def _scalar_of(dtype) -> str:
+    dt = str(dtype).replace("torch.", "")
+    table = {"float32": "s", "float64": "d", "complex64": "c", "complex128": "z"}
+    if dt not in table:
+        raise TypeError(f"unsupported dtype {dtype}")
+    return table[dt]
+
+
+def ptr(buf) -> int:
+    """Raw address of a numpy array or torch tensor."""
+    if buf is None:
+        return 0
+    if isinstance(buf, int):
+        return buf
+    if isinstance(buf, np.ndarray):
+        return buf.ctypes.data
+    return buf.data_ptr()  # torch tensor
+
+
+def _cplx_pair(v, real_t):
+    v = complex(v)
+    arr = (real_t * 2)(v.real, v.imag)
+    return arr
+
+
+def _stream_ptr(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class MMHandle:
+    """A Tiled-MM ``mm_handle<T>`` (owns streams and HBM tile buffers)."""
+
+    def __init__(self, scalar="d", streams=0, tile_m=0, tile_n=0, tile_k=0):
+        self.lib = N.load()
+        self.scalar = scalar
+        self._h = self.lib.cosma_gpu_tmm_make_context(scalar.encode(), streams, tile_m, tile_n, tile_k)
+        if not self._h:
+            N.check(self.lib.cosma_gpu_last_error() or N.CosmaGpuError(6, "make_context failed").code)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_method(self, method="native", slices=0):
+        m = N.METHODS[method] if isinstance(method, str) else int(method)
+        N.check(self.lib.cosma_gpu_tmm_set_method(self._h, m, slices))
+
+    def ozaki_info(self):
+        info = N.OzakiInfo()
+        N.check(self.lib.cosma_gpu_tmm_last_ozaki_info(self._h, C.byref(info)))
+        return info.as_dict()
+
+    def device_buffer_c(self) -> int:
+        return self.lib.cosma_gpu_tmm_device_buffer_c(self._h) or 0
+
+    def close(self):
+        if self._h:
+            self.lib.cosma_gpu_tmm_destroy_context(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_context(scalar="d", streams=0, tile_m=0, tile_n=0, tile_k=0) -> MMHandle:
+    return MMHandle(scalar, streams, tile_m, tile_n, tile_k)
+
+
+def gemm(handle: MMHandle, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc,
+         pin_host_buffers=True, copy_c_back=True):
+    """Tiled-MM gpu::gemm: C = alpha*op(A)*op(B) + beta*C on host or device buffers."""
+    lib = handle.lib
+    s = handle.scalar
+    ta, tb = transa.encode(), transb.encode()
+    args = (m, n, k)
+    if s in "sd":
+        f = lib.cosma_gpu_tmm_gemm_d if s == "d" else lib.cosma_gpu_tmm_gemm_s
+        st = f(handle.handle, ta, tb, *args, alpha, ptr(A), lda, ptr(B), ldb, beta, ptr(Cm), ldc,
+               int(pin_host_buffers), int(copy_c_back))
+    else:
+        rt = C.c_double if s == "z" else C.c_float
+        f = lib.cosma_gpu_tmm_gemm_z if s == "z" else lib.cosma_gpu_tmm_gemm_c
+        st = f(handle.handle, ta, tb, *args, _cplx_pair(alpha, rt), ptr(A), lda, ptr(B), ldb,
+               _cplx_pair(beta, rt), ptr(Cm), ldc, int(pin_host_buffers), int(copy_c_back))
+    N.check(st)
+
+
+def local_multiply(a, b, c, m, n, k, alpha, beta, copy_c_back=True, ctx: MMHandle | None = None):
+    """cosma::local_multiply on one rank: C = alpha*A*B + beta*C, ld = m, k, m."""
+    lib = N.load()
+    s = ctx.scalar if ctx is not None else _scalar_of(a.dtype)
+    h = ctx.handle if ctx is not None else None
+    if s in "sd":
+        f = lib.cosma_gpu_local_multiply_d if s == "d" else lib.cosma_gpu_local_multiply_s
+        st = f(h, ptr(a), ptr(b), ptr(c), m, n, k, alpha, beta, int(copy_c_back))
+    else:
+        rt = C.c_double if s == "z" else C.c_float
+        f = lib.cosma_gpu_local_multiply_z if s == "z" else lib.cosma_gpu_local_multiply_c
+        st = f(h, ptr(a), ptr(b), ptr(c), m, n, k, _cplx_pair(alpha, rt), _cplx_pair(beta, rt), int(copy_c_back))
+    N.check(st)
+
+
+def _ip(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def descinit(m, n, mb, nb, rsrc, csrc, ictxt, lld):
+    """The 9-integer ScaLAPACK array descriptor (dtype 1 = dense block-cyclic)."""
+    return np.array([1, ictxt, m, n, mb, nb, rsrc, csrc, lld], dtype=np.int32)
+
+
+def pxgemm(transa, transb, m, n, k, alpha, a, ia, ja, desca, b, ib, jb, descb, beta, c, ic, jc, descc,
+           scalar=None, prefix="p", suffix="_"):
+    """ScaLAPACK p?gemm on a 1x1 grid through the library's interposed symbol."""
+    lib = N.load()
+    s = scalar or _scalar_of(a.dtype)
+    name = f"{prefix}{s}gemm{suffix}" if prefix.islower() or prefix == "cosma_p" else f"{prefix}{s.upper()}GEMM{suffix}"
+    f = getattr(lib, name)
+    rt = C.c_double if s in "dz" else C.c_float
+    if s in "sd":
+        al, be = (rt * 1)(alpha), (rt * 1)(beta)
+    else:
+        al, be = _cplx_pair(alpha, rt), _cplx_pair(beta, rt)
+    da = np.ascontiguousarray(desca, dtype=np.int32)
+    db = np.ascontiguousarray(descb, dtype=np.int32)
+    dc = np.ascontiguousarray(descc, dtype=np.int32)
+    f(C.c_char_p(transa.encode()), C.c_char_p(transb.encode()), _ip(m), _ip(n), _ip(k), al, C.c_void_p(ptr(a)),
+      _ip(ia), _ip(ja), da.ctypes.data_as(C.c_void_p), C.c_void_p(ptr(b)), _ip(ib), _ip(jb),
+      db.ctypes.data_as(C.c_void_p), be, C.c_void_p(ptr(c)), _ip(ic), _ip(jc), dc.ctypes.data_as(C.c_void_p))
+    N.check(lib.cosma_gpu_last_error())
+
+
+def pxgemm_set_method(method="native"):
+    lib = N.load()
+    N.check(lib.cosma_gpu_pxgemm_set_method(N.METHODS[method] if isinstance(method, str) else int(method)))
+
+
+# ------------------------------------------------------ device-pointer API
+
+def gemm_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc, method="native", stream=None,
+                scalar=None):
+    """Stream-ordered GEMM on CUDA buffers (no synchronisation)."""
+    lib = N.load()
+    s = scalar or _scalar_of(A.dtype)
+    meth = N.METHODS[method] if isinstance(method, str) else int(method)
+    ta, tb, sp = transa.encode(), transb.encode(), _stream_ptr(stream)
+    if s == "d":
+        st = lib.cosma_gpu_dgemm_device(meth, ta, tb, m, n, k, alpha, ptr(A), lda, ptr(B), ldb, beta, ptr(Cm), ldc, sp)
+    elif s == "s":
+        st = lib.cosma_gpu_sgemm_device(meth, ta, tb, m, n, k, alpha, ptr(A), lda, ptr(B), ldb, beta, ptr(Cm), ldc, sp)
+    elif s == "z":
+        st = lib.cosma_gpu_zgemm_device(meth, ta, tb, m, n, k, _cplx_pair(alpha, C.c_double), ptr(A), lda, ptr(B),
+                                        ldb, _cplx_pair(beta, C.c_double), ptr(Cm), ldc, sp)
+    else:
+        st = lib.cosma_gpu_cgemm_device(meth, ta, tb, m, n, k, _cplx_pair(alpha, C.c_float), ptr(A), lda, ptr(B), ldb,
+                                        _cplx_pair(beta, C.c_float), ptr(Cm), ldc, sp)
+    N.check(st)
+
+
+def dgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc, slices=0, stream=None):
+    """FP64-accurate Ozaki-split DGEMM on CUDA buffers; returns the slice statistics."""
+    lib = N.load()
+    info = N.OzakiInfo()
+    N.check(lib.cosma_gpu_dgemm_ozaki_device(transa.encode(), transb.encode(), m, n, k, alpha, ptr(A), lda, ptr(B),
+                                             ldb, beta, ptr(Cm), ldc, slices, _stream_ptr(stream), C.byref(info)))
+    return info.as_dict()
+
+
+def pack(op, rows, cols, src, ld_src, dst, ld_dst, is_complex=False, elem_bytes=8, stream=None):
+    """COSTA 1x1 pack: dst(rows x cols) = op(src) on CUDA buffers."""
+    lib = N.load()
+    N.check(lib.costa_gpu_pack(op.encode(), int(is_complex), elem_bytes, rows, cols, ptr(src), ld_src, ptr(dst),
+                               ld_dst, _stream_ptr(stream)))
+
+
+def unpack(rows, cols, alpha, src, ld_src, beta, dst, ld_dst, scalar="d", stream=None):
+    """COSTA 1x1 back-transform: dst = alpha*src + beta*dst on CUDA buffers."""
+    lib = N.load()
+    sp = _stream_ptr(stream)
+    if scalar == "d":
+        st = lib.costa_gpu_unpack_d(rows, cols, alpha, ptr(src), ld_src, beta, ptr(dst), ld_dst, sp)
+    elif scalar == "s":
+        st = lib.costa_gpu_unpack_s(rows, cols, alpha, ptr(src), ld_src, beta, ptr(dst), ld_dst, sp)
+    elif scalar == "z":
+        st = lib.costa_gpu_unpack_z(rows, cols, _cplx_pair(alpha, C.c_double), ptr(src), ld_src,
+                                    _cplx_pair(beta, C.c_double), ptr(dst), ld_dst, sp)
+    else:
+        st = lib.costa_gpu_unpack_c(rows, cols, _cplx_pair(alpha, C.c_float), ptr(src), ld_src,
+                                    _cplx_pair(beta, C.c_float), ptr(dst), ld_dst, sp)
+    N.check(st)

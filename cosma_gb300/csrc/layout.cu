@@ -1,0 +1,335 @@
+// COSTA layout transforms on a 1x1 process grid, as GPU kernels.
+//
+// On one rank a ScaLAPACK block-cyclic matrix is a single column-major
+// buffer with leading dimension LLD (block-cyclic owner (i/mb) % 1 == 0 and
+// local index (i/(mb*1))*mb + i%mb == i, the map restated in
+// utils/pxgemm_utils.hpp:66-90), so costa::transformer's pack of a
+// sub-matrix into COSMA's blocked layout (src/cosma/cosma_pxgemm.cpp:212-249,
+// 338-343) is   dst(rows x cols, ld = rows) = op(src(ia:, ja:))   with op in
+// {N, T, C}, and the back-transform of C (cosma_pxgemm.cpp:362-364) is
+// dst = alpha*src + beta*dst.
+//
+// * pack: pure data movement, bit-exact (conjugation flips the sign bit of
+//   the imaginary part, which is IEEE negation).  Transposing packs stage a
+//   64x64-element tile (32x32 for 16-byte elements) through padded shared
+//   memory so that both the HBM read and the HBM write are full-line
+//   coalesced; non-transposing packs are a 16-byte-vectorised 2-D copy.
+// * unpack: dst = fl(fl(alpha*src) + fl(beta*dst)) without FMA contraction;
+//   dst is never read when beta == 0 (the reference's test pre-fills C with
+//   NaN in that case, utils/pxgemm_utils.hpp:604-614).
+#include "common.cuh"
+#include "runtime.hpp"
+
+namespace cgb {
+namespace {
+
+// 16-byte element carrier (complex double)
+struct alignas(16) U128 { unsigned long long lo, hi; };
+
+template <class U> __device__ __forceinline__ U conj_bits(U v);
+template <> __device__ __forceinline__ unsigned long long conj_bits(unsigned long long v) {
+    return v ^ 0x8000000000000000ull;  // complex float: imaginary float in the high word
+}
+template <> __device__ __forceinline__ U128 conj_bits(U128 v) {
+    v.hi ^= 0x8000000000000000ull;
+    return v;
+}
+template <> __device__ __forceinline__ unsigned conj_bits(unsigned v) { return v; }
+
+// Transpose tile edge in elements: 64 for 4/8-byte elements (33 KB of
+// static shared memory), 32 for 16-byte elements.  Rows are padded by one
+// element, which makes the column-wise shared reads conflict-free for 4-byte
+// elements and minimal-wavefront for 8/16-byte elements.
+template <class U> struct TileEdge { static constexpr int value = sizeof(U) == 16 ? 32 : 64; };
+constexpr int kTransposeThreads = 256;
+
+// dst[i + j*ldd] = op(src)[i, j] = src[j + i*lds]   (op = T or C)
+// Reads run along src's contiguous dimension, writes along dst's.
+template <class U, bool CONJ>
+__global__ void __launch_bounds__(kTransposeThreads) transpose_kernel(int64_t rows, int64_t cols,
+                                                                      const U* __restrict__ src, int64_t lds,
+                                                                      U* __restrict__ dst, int64_t ldd) {
+    constexpr int TT = TileEdge<U>::value;
+    constexpr int NY = kTransposeThreads / TT;
+    __shared__ U tile[TT][TT + 1];
+    const int64_t i0 = (int64_t)blockIdx.x * TT;  // dst rows = src cols
+    const int64_t j0 = (int64_t)blockIdx.y * TT;  // dst cols = src rows
+    const int tx = threadIdx.x % TT, ty = threadIdx.x / TT;
+#pragma unroll 4
+    for (int r = ty; r < TT; r += NY) {
+        int64_t j = j0 + tx, i = i0 + r;
+        if (j < cols && i < rows) tile[r][tx] = src[j + i * lds];
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int r = ty; r < TT; r += NY) {
+        int64_t i = i0 + tx, j = j0 + r;
+        if (i < rows && j < cols) {
+            U v = tile[tx][r];
+            if (CONJ) v = conj_bits(v);
+            dst[i + j * ldd] = v;
+        }
+    }
+}
+
+// dst[i + j*ldd] = src[i + j*lds]   (op = N), column-per-warp vectorised copy.
+template <class U>
+__global__ void copy2d_kernel(int64_t rows, int64_t cols, const U* __restrict__ src, int64_t lds,
+                              U* __restrict__ dst, int64_t ldd) {
+    const int64_t total_cols = cols;
+    for (int64_t j = blockIdx.y; j < total_cols; j += gridDim.y) {
+        const U* s = src + j * lds;
+        U* d = dst + j * ldd;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
+            d[i] = s[i];
+    }
+}
+
+// 16-byte vectorised column copy when both columns are 16-byte aligned.
+__global__ void copy2d_vec16_kernel(int64_t rows_bytes16, int64_t cols, const uint4* __restrict__ src,
+                                    int64_t lds16, uint4* __restrict__ dst, int64_t ldd16) {
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y) {
+        const uint4* s = src + j * lds16;
+        uint4* d = dst + j * ldd16;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows_bytes16;
+             i += (int64_t)gridDim.x * blockDim.x)
+            d[i] = s[i];
+    }
+}
+
+template <class U>
+__global__ void conj_copy2d_kernel(int64_t rows, int64_t cols, const U* __restrict__ src, int64_t lds,
+                                   U* __restrict__ dst, int64_t ldd) {
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
+            dst[i + j * ldd] = conj_bits(src[i + j * lds]);
+}
+
+// ---------------------------------------------------------------- unpack
+template <class R>
+__device__ __forceinline__ R mul_rn(R a, R b);
+template <> __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+template <class R>
+__device__ __forceinline__ R add_rn(R a, R b);
+template <> __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+template <class R>
+__device__ __forceinline__ R sub_rn(R a, R b);
+template <> __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+// real: d = fl(fl(alpha*s) + fl(beta*d)); beta == 0 -> d = fl(alpha*s)
+template <class R>
+__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, const R* __restrict__ src, int64_t lds,
+                                   R beta, R* __restrict__ dst, int64_t ldd, int read_dst) {
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+            R v = mul_rn(alpha, src[i + j * lds]);
+            if (read_dst) v = add_rn(v, mul_rn(beta, dst[i + j * ldd]));
+            dst[i + j * ldd] = v;
+        }
+}
+
+// complex: x*y = (xr*yr - xi*yi) + (xr*yi + xi*yr) i, every product and sum
+// rounded separately (no contraction); d = fl(alpha*s + beta*d) componentwise.
+template <class R, class V>
+__device__ __forceinline__ V cmul_rn(R ar, R ai, V s) {
+    V out;
+    out.x = sub_rn(mul_rn(ar, s.x), mul_rn(ai, s.y));
+    out.y = add_rn(mul_rn(ar, s.y), mul_rn(ai, s.x));
+    return out;
+}
+template <class R, class V>
+__global__ void unpack_cplx_kernel(int64_t rows, int64_t cols, R ar, R ai, const V* __restrict__ src, int64_t lds,
+                                   R br, R bi, V* __restrict__ dst, int64_t ldd, int read_dst) {
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+            V v = cmul_rn<R, V>(ar, ai, src[i + j * lds]);
+            if (read_dst) {
+                V w = cmul_rn<R, V>(br, bi, dst[i + j * ldd]);
+                v.x = add_rn(v.x, w.x);
+                v.y = add_rn(v.y, w.y);
+            }
+            dst[i + j * ldd] = v;
+        }
+}
+
+// C <- beta * C (k == 0 or alpha == 0 corner case of p?gemm / gemm).
+// beta == 0 writes zeros without reading C.
+template <class R>
+__global__ void scale_real_kernel(int64_t rows, int64_t cols, R beta, R* C, int64_t ldc) {
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x)
+            C[i + j * ldc] = (beta == R(0)) ? R(0) : mul_rn(beta, C[i + j * ldc]);
+}
+template <class R, class V>
+__global__ void scale_cplx_kernel(int64_t rows, int64_t cols, R br, R bi, V* C, int64_t ldc) {
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+            V v;
+            if (br == R(0) && bi == R(0)) { v.x = R(0); v.y = R(0); }
+            else v = cmul_rn<R, V>(br, bi, C[i + j * ldc]);
+            C[i + j * ldc] = v;
+        }
+}
+
+dim3 grid2d(int64_t rows, int64_t cols, int threads) {
+    int64_t bx = ceil_div(rows, threads);
+    if (bx > 64) bx = 64;
+    int64_t by = cols < 65535 ? cols : 65535;
+    if (by < 1) by = 1;
+    if (bx < 1) bx = 1;
+    return dim3((unsigned)bx, (unsigned)by);
+}
+
+template <class U>
+int pack_typed(int op, int64_t rows, int64_t cols, const void* src, int64_t lds, void* dst, int64_t ldd,
+               cudaStream_t s) {
+    if (op == 0) {
+        const size_t eb = sizeof(U);
+        if (((uintptr_t)src % 16 == 0) && ((uintptr_t)dst % 16 == 0) && ((lds * eb) % 16 == 0) &&
+            ((ldd * eb) % 16 == 0) && ((rows * eb) % 16 == 0)) {
+            int64_t r16 = rows * eb / 16;
+            copy2d_vec16_kernel<<<grid2d(r16, cols, 256), 256, 0, s>>>(r16, cols, (const uint4*)src, lds * eb / 16,
+                                                                         (uint4*)dst, ldd * eb / 16);
+        } else {
+            copy2d_kernel<U><<<grid2d(rows, cols, 256), 256, 0, s>>>(rows, cols, (const U*)src, lds, (U*)dst, ldd);
+        }
+    } else if (op == 3) {  // conjugate without transpose (internal use)
+        conj_copy2d_kernel<U><<<grid2d(rows, cols, 256), 256, 0, s>>>(rows, cols, (const U*)src, lds, (U*)dst, ldd);
+    } else {
+        constexpr int TT = TileEdge<U>::value;
+        dim3 grid((unsigned)ceil_div(rows, TT), (unsigned)ceil_div(cols, TT));
+        if (grid.y > 65535) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "pack: too many columns");
+        if (op == 2)
+            transpose_kernel<U, true><<<grid, kTransposeThreads, 0, s>>>(rows, cols, (const U*)src, lds, (U*)dst, ldd);
+        else
+            transpose_kernel<U, false><<<grid, kTransposeThreads, 0, s>>>(rows, cols, (const U*)src, lds, (U*)dst, ldd);
+    }
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace
+
+int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t cols, const void* src, int64_t lds,
+                void* dst, int64_t ldd, cudaStream_t s) {
+    if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    if (op == 2 && !is_complex) op = 1;  // conjugate transpose of real data is a transpose
+    if (elem_bytes == 4 || elem_bytes == 8 || elem_bytes == 16) {
+        if (((uintptr_t)src | (uintptr_t)dst) % (uintptr_t)elem_bytes)
+            return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "pack: buffers must be aligned to the element size");
+    }
+    switch (elem_bytes) {
+        case 4: return pack_typed<unsigned>(op, rows, cols, src, lds, dst, ldd, s);
+        case 8: return pack_typed<unsigned long long>(op, rows, cols, src, lds, dst, ldd, s);
+        case 16: return pack_typed<U128>(op, rows, cols, src, lds, dst, ldd, s);
+    }
+    return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "pack: elem_bytes must be 4, 8 or 16");
+}
+
+int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
+                  const double* beta, void* dst, int64_t ldd, cudaStream_t s) {
+    if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    const uintptr_t align = sc == Scalar::Z ? 16 : (sc == Scalar::S ? 4 : 8);
+    if (((uintptr_t)src | (uintptr_t)dst) % align)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "unpack: buffers must be aligned to the element size");
+    const int read_dst = !(beta[0] == 0.0 && (!scalar_complex(sc) || beta[1] == 0.0));
+    dim3 g = grid2d(rows, cols, 256);
+    switch (sc) {
+        case Scalar::D:
+            unpack_real_kernel<double><<<g, 256, 0, s>>>(rows, cols, alpha[0], (const double*)src, lds, beta[0],
+                                                         (double*)dst, ldd, read_dst);
+            break;
+        case Scalar::S:
+            unpack_real_kernel<float><<<g, 256, 0, s>>>(rows, cols, (float)alpha[0], (const float*)src, lds,
+                                                        (float)beta[0], (float*)dst, ldd, read_dst);
+            break;
+        case Scalar::Z:
+            unpack_cplx_kernel<double, double2><<<g, 256, 0, s>>>(rows, cols, alpha[0], alpha[1],
+                                                                  (const double2*)src, lds, beta[0], beta[1],
+                                                                  (double2*)dst, ldd, read_dst);
+            break;
+        case Scalar::C:
+            unpack_cplx_kernel<float, float2><<<g, 256, 0, s>>>(rows, cols, (float)alpha[0], (float)alpha[1],
+                                                                (const float2*)src, lds, (float)beta[0],
+                                                                (float)beta[1], (float2*)dst, ldd, read_dst);
+            break;
+    }
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
+}
+
+int scale_matrix_device(Scalar sc, int64_t rows, int64_t cols, const double* beta, void* C, int64_t ldc,
+                        cudaStream_t s) {
+    if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    const bool one = beta[0] == 1.0 && (!scalar_complex(sc) || beta[1] == 0.0);
+    if (one) return COSMA_GPU_SUCCESS;
+    const uintptr_t align = sc == Scalar::Z ? 16 : (sc == Scalar::S ? 4 : 8);
+    if ((uintptr_t)C % align)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "scale: C must be aligned to the element size");  // scale_matrix returns early for beta == 1 (cosma_pxgemm.cpp:399)
+    dim3 g = grid2d(rows, cols, 256);
+    switch (sc) {
+        case Scalar::D: scale_real_kernel<double><<<g, 256, 0, s>>>(rows, cols, beta[0], (double*)C, ldc); break;
+        case Scalar::S: scale_real_kernel<float><<<g, 256, 0, s>>>(rows, cols, (float)beta[0], (float*)C, ldc); break;
+        case Scalar::Z:
+            scale_cplx_kernel<double, double2><<<g, 256, 0, s>>>(rows, cols, beta[0], beta[1], (double2*)C, ldc);
+            break;
+        case Scalar::C:
+            scale_cplx_kernel<float, float2><<<g, 256, 0, s>>>(rows, cols, (float)beta[0], (float)beta[1],
+                                                               (float2*)C, ldc);
+            break;
+    }
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace cgb
+
+extern "C" {
+
+int costa_gpu_pack(char op, int is_complex, int elem_bytes, int64_t rows, int64_t cols, const void* src,
+                   int64_t ld_src, void* dst, int64_t ld_dst, void* stream) {
+    cgb::clear_error();
+    int o = cgb::parse_op(op);
+    if (o < 0) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "costa_gpu_pack: op must be N, T or C");
+    if (rows < 0 || cols < 0) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "costa_gpu_pack: negative size");
+    // src is (rows x cols) for N, (cols x rows) for T/C
+    int64_t src_rows = o == 0 ? rows : cols;
+    if (ld_src < (src_rows > 1 ? src_rows : 1) || ld_dst < (rows > 1 ? rows : 1))
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "costa_gpu_pack: leading dimension too small");
+    return cgb::pack_device(o, is_complex != 0, elem_bytes, rows, cols, src, ld_src, dst, ld_dst,
+                            (cudaStream_t)stream);
+}
+
+static int unpack_common(cgb::Scalar sc, int64_t rows, int64_t cols, const double* a, const void* src, int64_t lds,
+                         const double* b, void* dst, int64_t ldd, void* stream) {
+    cgb::clear_error();
+    if (rows < 0 || cols < 0 || lds < (rows > 1 ? rows : 1) || ldd < (rows > 1 ? rows : 1))
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "costa_gpu_unpack: bad size or leading dimension");
+    return cgb::unpack_device(sc, rows, cols, a, src, lds, b, dst, ldd, (cudaStream_t)stream);
+}
+
+int costa_gpu_unpack_d(int64_t rows, int64_t cols, double alpha, const double* src, int64_t ld_src, double beta,
+                       double* dst, int64_t ld_dst, void* stream) {
+    double a[2] = {alpha, 0}, b[2] = {beta, 0};
+    return unpack_common(cgb::Scalar::D, rows, cols, a, src, ld_src, b, dst, ld_dst, stream);
+}
+int costa_gpu_unpack_s(int64_t rows, int64_t cols, float alpha, const float* src, int64_t ld_src, float beta,
+                       float* dst, int64_t ld_dst, void* stream) {
+    double a[2] = {alpha, 0}, b[2] = {beta, 0};
+    return unpack_common(cgb::Scalar::S, rows, cols, a, src, ld_src, b, dst, ld_dst, stream);
+}
+int costa_gpu_unpack_z(int64_t rows, int64_t cols, const double* alpha, const double* src, int64_t ld_src,
+                       const double* beta, double* dst, int64_t ld_dst, void* stream) {
+    double a[2] = {alpha[0], alpha[1]}, b[2] = {beta[0], beta[1]};
+    return unpack_common(cgb::Scalar::Z, rows, cols, a, src, ld_src, b, dst, ld_dst, stream);
+}
+int costa_gpu_unpack_c(int64_t rows, int64_t cols, const float* alpha, const float* src, int64_t ld_src,
+                       const float* beta, float* dst, int64_t ld_dst, void* stream) {
+    double a[2] = {alpha[0], alpha[1]}, b[2] = {beta[0], beta[1]};
+    return unpack_common(cgb::Scalar::C, rows, cols, a, src, ld_src, b, dst, ld_dst, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,78 @@
+// Host-side runtime declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace cgb {
+
+bool env_bool(const char* name, bool dflt);
+long long env_ll(const char* name, long long dflt);
+bool env_verbose();
+int default_streams();
+int default_tile_m();
+int default_tile_n();
+int default_tile_k();
+bool default_pinning();
+int default_method();
+
+// Scalar kinds of the four GEMM flavours.
+enum class Scalar { S, D, C, Z };
+
+inline size_t scalar_bytes(Scalar s) {
+    switch (s) {
+        case Scalar::S: return 4;
+        case Scalar::D: return 8;
+        case Scalar::C: return 8;
+        case Scalar::Z: return 16;
+    }
+    return 8;
+}
+inline bool scalar_complex(Scalar s) { return s == Scalar::C || s == Scalar::Z; }
+
+// op(X) codes: 0 = 'N', 1 = 'T', 2 = 'C'; -1 for an invalid flag.
+inline int parse_op(char c) {
+    switch (c) {
+        case 'N': case 'n': return 0;
+        case 'T': case 't': return 1;
+        case 'C': case 'c': return 2;
+    }
+    return -1;
+}
+
+// Reusable grow-only device buffer (stream-ordered allocation).
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int reserve(size_t need, cudaStream_t stream);
+    void release();
+    ~DeviceBuffer() { release(); }
+};
+
+// Generic GEMM description on device pointers.  Complex scalars use
+// alpha[0..1] / beta[0..1]; real scalars use alpha[0] / beta[0].
+struct GemmDesc {
+    Scalar scalar;
+    int opa, opb;           // 0 N, 1 T, 2 C
+    int64_t m, n, k;
+    double alpha[2], beta[2];
+    const void* A; int64_t lda;
+    const void* B; int64_t ldb;
+    void* C; int64_t ldc;
+};
+
+// Device-level entry points implemented in the .cu files.
+int native_gemm(const GemmDesc& g, cudaStream_t stream);          // dmma_gemm.cu
+int scale_matrix_device(Scalar s, int64_t rows, int64_t cols, const double* beta, void* C,
+                        int64_t ldc, cudaStream_t stream);        // layout.cu
+int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream,
+                cosma_gpu_ozaki_info* info);                     // ozaki.cu
+int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
+
+// Dispatches one device-pointer GEMM by method (handles the k == 0 /
+// alpha == 0 corner cases).  Defined in gemm_dispatch.cpp.
+int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t stream,
+                cosma_gpu_ozaki_info* info);
+
+}  // namespace cgb

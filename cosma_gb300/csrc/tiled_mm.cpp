@@ -1,0 +1,474 @@
+// Tiled-MM-compatible GEMM engine: the handle, the host<->HBM tile streamer
+// and the COSMA local_multiply entry points.
+//
+// Reference behaviour (Tiled-MM v2.3.2 as used by COSMA):
+//  * gpu::make_context<T>(streams, tile_m, tile_n, tile_k) creates a handle
+//    owning device tile buffers and streams (src/cosma/context.cpp:24-25,45);
+//    device memory streams*(tm*tk + tk*tn + tm*tn) elements (README.md:362-365).
+//  * gpu::gemm(handle, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+//    pin, copy_c_back) computes C = alpha*op(A)*op(B) + beta*C on host
+//    matrices: C is cut into tm x tn tiles and K into tk slabs, tiles are
+//    dealt round-robin to the streams, each tile copies its A/B slabs in,
+//    multiplies (beta on the first K slab, 1 afterwards) and copies C back
+//    (call site src/cosma/local_multiply.cpp:245-260).
+//  * cosma::local_multiply pins A, B, C once (memory_pool::pin ->
+//    cudaHostRegister, re-registered when a buffer grows;
+//    src/cosma/pinned_buffers.cpp:6-35) and calls gpu::gemm with 'N','N'
+//    and ld = m, k, m (src/cosma/local_multiply.cpp:300-381).
+//
+// GB300 design: one process drives one GPU with 280 GB of HBM, so the
+// default tile covers any in-core problem up to 32768 in a single piece and
+// the matrices cross the C2C link exactly once; larger problems stream tiles
+// over several streams so that copies of one tile overlap the GEMM of
+// another.  Device pointers are detected and used in place (no copies).
+#include "common.cuh"
+#include "runtime.hpp"
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
+namespace cgb {
+GemmDesc make_gemm_desc(Scalar s, char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,
+                        const void* A, int64_t lda, const void* B, int64_t ldb, const double* beta, void* C,
+                        int64_t ldc);
+}
+
+struct cosma_gpu_mm_handle {
+    cgb::Scalar scalar = cgb::Scalar::D;
+    int n_streams = 3, tile_m = 0, tile_n = 0, tile_k = 0;
+    int method = COSMA_GPU_METHOD_AUTO, slices = 0;
+    int device = 0;
+    std::vector<cudaStream_t> streams;
+    std::vector<cgb::DeviceBuffer> bufA, bufB, bufC;
+    cgb::DeviceBuffer full_c;
+    void* last_device_c = nullptr;
+    std::map<uintptr_t, size_t> pinned;  // registered host ranges (base -> bytes)
+    std::mutex mu;
+    cosma_gpu_ozaki_info last_info{0, 0, 0, 0, 0.0};
+};
+
+namespace cgb {
+namespace {
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Page-locks [ptr, ptr+bytes) for the copies of one call.
+//
+// The reference keeps registrations until its context is destroyed and
+// re-registers a pointer only when it grows (pinned_buffers::add,
+// src/cosma/pinned_buffers.cpp:6-35).  That is safe for COSMA's own memory
+// pool, which owns the buffers, but not for callers that free a buffer and
+// get a new one at the same address: the driver would keep the stale
+// registration.  So registrations are scoped to the call by default
+// (registered ranges are recorded in `scoped` and released by the caller of
+// pin_range); COSMA_GPU_PIN_CACHE=ON restores the reference's
+// keep-until-destroyed policy for callers whose buffers outlive the handle.
+// Memory that its owner already page-locked is used as it is.
+int pin_range(cosma_gpu_mm_handle* h, const void* ptr, size_t bytes, std::vector<void*>& scoped) {
+    if (!ptr || bytes == 0) return COSMA_GPU_SUCCESS;
+    static const bool cache = env_bool("COSMA_GPU_PIN_CACHE", false);
+    uintptr_t key = (uintptr_t)ptr;
+    if (cache) {
+        auto it = h->pinned.find(key);
+        if (it != h->pinned.end()) {
+            if (it->second >= bytes) return COSMA_GPU_SUCCESS;
+            cudaHostUnregister((void*)ptr);
+            cudaGetLastError();
+            h->pinned.erase(it);
+        }
+    }
+    cudaError_t e = cudaHostRegister((void*)ptr, bytes, cudaHostRegisterDefault);
+    if (e == cudaErrorHostMemoryAlreadyRegistered) {  // page-locked by its owner
+        cudaGetLastError();
+        return COSMA_GPU_SUCCESS;
+    }
+    if (e != cudaSuccess) {
+        // Pinning is an optimisation: memory that cannot be registered still
+        // moves through staged pageable copies.
+        cudaGetLastError();
+        if (env_verbose()) std::fprintf(stderr, "[cosma_gb300] cudaHostRegister failed: %s\n", cudaGetErrorString(e));
+        return COSMA_GPU_SUCCESS;
+    }
+    if (cache) h->pinned[key] = bytes;
+    else scoped.push_back((void*)ptr);
+    return COSMA_GPU_SUCCESS;
+}
+
+void unpin_scoped(std::vector<void*>& scoped) {
+    for (void* p : scoped) cudaHostUnregister(p);
+    scoped.clear();
+    cudaGetLastError();
+}
+
+size_t span_bytes(int64_t rows, int64_t cols, int64_t ld, size_t es) {
+    if (rows <= 0 || cols <= 0) return 0;
+    return ((size_t)(cols - 1) * (size_t)ld + (size_t)rows) * es;
+}
+
+int copy2d(void* dst, int64_t dld, const void* src, int64_t sld, int64_t rows, int64_t cols, size_t es,
+           cudaMemcpyKind kind, cudaStream_t s) {
+    if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    CGB_CUDA(cudaMemcpy2DAsync(dst, (size_t)dld * es, src, (size_t)sld * es, (size_t)rows * es, (size_t)cols, kind, s));
+    return COSMA_GPU_SUCCESS;
+}
+
+bool is_zero(const double* v, Scalar s) { return v[0] == 0.0 && (!scalar_complex(s) || v[1] == 0.0); }
+bool is_one(const double* v, Scalar s) { return v[0] == 1.0 && (!scalar_complex(s) || v[1] == 0.0); }
+
+}  // namespace
+
+int handle_init(cosma_gpu_mm_handle* h) {
+    CGB_CUDA(cudaGetDevice(&h->device));
+    h->streams.resize(h->n_streams);
+    for (auto& s : h->streams) CGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    h->bufA.resize(h->n_streams);
+    h->bufB.resize(h->n_streams);
+    h->bufC.resize(h->n_streams);
+    return COSMA_GPU_SUCCESS;
+}
+
+int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int opa, int opb, int64_t m, int64_t n,
+                     int64_t k, const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
+                     const double* beta, void* C, int64_t ldc, bool dA, bool dB, bool dC, bool trivial,
+                     bool copy_c_back, cosma_gpu_ozaki_info* info);
+
+// C = alpha*op(A)*op(B) + beta*C with any mix of host and device pointers.
+int tmm_gemm(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int64_t m, int64_t n, int64_t k,
+             const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb, const double* beta,
+             void* C, int64_t ldc, bool pin, bool copy_c_back) {
+    if (!h) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: null handle");
+    if (h->scalar != sc) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: handle scalar type mismatch");
+    const int opa = parse_op(ta), opb = parse_op(tb);
+    if (opa < 0 || opb < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: op must be N, T or C");
+    if (m < 0 || n < 0 || k < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: negative size");
+    if (m == 0 || n == 0) return COSMA_GPU_SUCCESS;
+    const int64_t a_rows = opa == 0 ? m : k, a_cols = opa == 0 ? k : m;
+    const int64_t b_rows = opb == 0 ? k : n, b_cols = opb == 0 ? n : k;
+    if (ldc < std::max<int64_t>(1, m) || (k > 0 && (lda < std::max<int64_t>(1, a_rows) || ldb < std::max<int64_t>(1, b_rows))))
+        return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: leading dimension too small");
+
+    std::lock_guard<std::mutex> lock(h->mu);
+    CGB_CUDA(cudaSetDevice(h->device));
+    const size_t es = scalar_bytes(sc);
+    const bool dA = is_device_ptr(A), dB = is_device_ptr(B), dC = is_device_ptr(C);
+    const bool trivial = (k == 0) || is_zero(alpha, sc);
+    cosma_gpu_ozaki_info* info = &h->last_info;
+    *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0};
+
+    if (trivial && is_one(beta, sc)) return COSMA_GPU_SUCCESS;  // C unchanged
+    if (dC && (trivial || (dA && dB))) {  // everything already in HBM
+        GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        CGB_CHECK(gemm_device(g, h->method, h->slices, h->streams[0], info));
+        CGB_CUDA(cudaStreamSynchronize(h->streams[0]));
+        h->last_device_c = C;
+        return COSMA_GPU_SUCCESS;
+    }
+
+    std::vector<void*> scoped;
+    if (pin) {
+        if (!dA && !trivial) pin_range(h, A, span_bytes(a_rows, a_cols, lda, es), scoped);
+        if (!dB && !trivial) pin_range(h, B, span_bytes(b_rows, b_cols, ldb, es), scoped);
+        if (!dC) pin_range(h, C, span_bytes(m, n, ldc, es), scoped);
+    }
+    int status = tmm_stream_tiles(h, sc, ta, tb, opa, opb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, dA, dB, dC,
+                                  trivial, copy_c_back, info);
+    unpin_scoped(scoped);
+    return status;
+}
+
+// The tile loop of tmm_gemm (host or mixed pointers).
+int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int opa, int opb, int64_t m, int64_t n,
+                     int64_t k, const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
+                     const double* beta, void* C, int64_t ldc, bool dA, bool dB, bool dC, bool trivial,
+                     bool copy_c_back, cosma_gpu_ozaki_info* info) {
+    const size_t es = scalar_bytes(sc);
+
+    // Tile plan: tiles never exceed the handle's limits; shrink the largest
+    // dimension until the per-stream buffers fit in 60% of free HBM.
+    int64_t tm = std::min<int64_t>(m, h->tile_m), tn = std::min<int64_t>(n, h->tile_n);
+    int64_t tk = std::min<int64_t>(std::max<int64_t>(k, 1), h->tile_k);
+    size_t free_b = 0, total_b = 0;
+    CGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const int S = h->n_streams;
+    for (;;) {
+        size_t per = ((dA ? 0 : (size_t)tm * tk) + (dB ? 0 : (size_t)tk * tn) + (dC ? 0 : (size_t)tm * tn)) * es;
+        size_t have = 0;
+        for (int s = 0; s < S; ++s) have += h->bufA[s].bytes + h->bufB[s].bytes + h->bufC[s].bytes;
+        if (per * S <= (size_t)(0.6 * (double)(free_b + have)) || (tm <= 256 && tn <= 256 && tk <= 256)) break;
+        if (tk >= tm && tk >= tn) tk = (tk + 1) / 2;
+        else if (tm >= tn) tm = (tm + 1) / 2;
+        else tn = (tn + 1) / 2;
+    }
+    const int64_t ntm = ceil_div(m, tm), ntn = ceil_div(n, tn), ntk = trivial ? 0 : ceil_div(k, tk);
+    const int64_t ntiles = ntm * ntn;
+    const int used_streams = (int)std::min<int64_t>(S, ntiles);
+    for (int s = 0; s < used_streams; ++s) {
+        if (!dA && !trivial) CGB_CHECK(h->bufA[s].reserve((size_t)tm * tk * es, h->streams[s]));
+        if (!dB && !trivial) CGB_CHECK(h->bufB[s].reserve((size_t)tk * tn * es, h->streams[s]));
+        if (!dC) CGB_CHECK(h->bufC[s].reserve((size_t)tm * tn * es, h->streams[s]));
+    }
+    const bool keep_on_device = !dC && !copy_c_back;
+    if (keep_on_device) CGB_CHECK(h->full_c.reserve((size_t)m * n * es, h->streams[0]));
+    CGB_CUDA(cudaDeviceSynchronize());  // buffers from any earlier call are idle
+
+    const double one[2] = {1.0, 0.0};
+    int status = COSMA_GPU_SUCCESS;
+    for (int64_t t = 0; t < ntiles && status == COSMA_GPU_SUCCESS; ++t) {
+        const int s_idx = (int)(t % used_streams);
+        cudaStream_t st = h->streams[s_idx];
+        const int64_t ti = t % ntm, tj = t / ntm;
+        const int64_t i0 = ti * tm, j0 = tj * tn;
+        const int64_t mi = std::min(tm, m - i0), nj = std::min(tn, n - j0);
+        // C tile
+        char* cdev;
+        int64_t cld;
+        if (dC) {
+            cdev = (char*)C + (i0 + j0 * ldc) * es;
+            cld = ldc;
+        } else {
+            cdev = (char*)h->bufC[s_idx].ptr;
+            cld = mi;
+            if (!is_zero(beta, sc))
+                if ((status = copy2d(cdev, cld, (const char*)C + (i0 + j0 * ldc) * es, ldc, mi, nj, es,
+                                     cudaMemcpyHostToDevice, st)))
+                    break;
+        }
+        if (trivial) {
+            status = scale_matrix_device(sc, mi, nj, beta, cdev, cld, st);
+        }
+        for (int64_t kt = 0; kt < ntk && status == COSMA_GPU_SUCCESS; ++kt) {
+            const int64_t l0 = kt * tk, kk = std::min(tk, k - l0);
+            // op(A) tile rows [i0, i0+mi) x cols [l0, l0+kk)
+            const char* adev;
+            int64_t ald;
+            if (opa == 0) {
+                const char* src = (const char*)A + (i0 + l0 * lda) * es;
+                if (dA) { adev = src; ald = lda; }
+                else {
+                    adev = (const char*)h->bufA[s_idx].ptr; ald = mi;
+                    if ((status = copy2d((void*)adev, ald, src, lda, mi, kk, es, cudaMemcpyHostToDevice, st))) break;
+                }
+            } else {
+                const char* src = (const char*)A + (l0 + i0 * lda) * es;
+                if (dA) { adev = src; ald = lda; }
+                else {
+                    adev = (const char*)h->bufA[s_idx].ptr; ald = kk;
+                    if ((status = copy2d((void*)adev, ald, src, lda, kk, mi, es, cudaMemcpyHostToDevice, st))) break;
+                }
+            }
+            // op(B) tile rows [l0, l0+kk) x cols [j0, j0+nj)
+            const char* bdev;
+            int64_t bld;
+            if (opb == 0) {
+                const char* src = (const char*)B + (l0 + j0 * ldb) * es;
+                if (dB) { bdev = src; bld = ldb; }
+                else {
+                    bdev = (const char*)h->bufB[s_idx].ptr; bld = kk;
+                    if ((status = copy2d((void*)bdev, bld, src, ldb, kk, nj, es, cudaMemcpyHostToDevice, st))) break;
+                }
+            } else {
+                const char* src = (const char*)B + (j0 + l0 * ldb) * es;
+                if (dB) { bdev = src; bld = ldb; }
+                else {
+                    bdev = (const char*)h->bufB[s_idx].ptr; bld = nj;
+                    if ((status = copy2d((void*)bdev, bld, src, ldb, nj, kk, es, cudaMemcpyHostToDevice, st))) break;
+                }
+            }
+            GemmDesc g = make_gemm_desc(sc, ta, tb, mi, nj, kk, alpha, adev, ald, bdev, bld, kt == 0 ? beta : one,
+                                        cdev, cld);
+            cosma_gpu_ozaki_info ti_info;
+            status = gemm_device(g, h->method, h->slices, st, &ti_info);
+            if (ti_info.slices) *info = ti_info;
+        }
+        if (status) break;
+        if (!dC) {
+            if (keep_on_device)
+                status = copy2d((char*)h->full_c.ptr + (i0 + j0 * m) * es, m, cdev, cld, mi, nj, es,
+                                cudaMemcpyDeviceToDevice, st);
+            else
+                status = copy2d((char*)C + (i0 + j0 * ldc) * es, ldc, cdev, cld, mi, nj, es, cudaMemcpyDeviceToHost, st);
+        }
+    }
+    for (int s = 0; s < used_streams; ++s) {
+        cudaError_t e = cudaStreamSynchronize(h->streams[s]);
+        if (e != cudaSuccess && status == COSMA_GPU_SUCCESS) status = cuda_status(e, "cudaStreamSynchronize");
+    }
+    h->last_device_c = dC ? C : (keep_on_device ? h->full_c.ptr : nullptr);
+    return status;
+}
+
+}  // namespace cgb
+
+// ------------------------------------------------------------------ C ABI
+namespace {
+
+bool parse_scalar(char c, cgb::Scalar* s) {
+    switch (c) {
+        case 's': case 'S': *s = cgb::Scalar::S; return true;
+        case 'd': case 'D': *s = cgb::Scalar::D; return true;
+        case 'c': case 'C': *s = cgb::Scalar::C; return true;
+        case 'z': case 'Z': *s = cgb::Scalar::Z; return true;
+    }
+    return false;
+}
+
+std::mutex g_singleton_mu;
+cosma_gpu_mm_handle* g_singletons[4] = {nullptr, nullptr, nullptr, nullptr};
+bool g_pin_default = true;
+
+}  // namespace
+
+extern "C" {
+
+cosma_gpu_mm_handle* cosma_gpu_tmm_make_context(char scalar, int streams, int tile_m, int tile_n, int tile_k) {
+    cgb::clear_error();
+    cgb::Scalar s;
+    if (!parse_scalar(scalar, &s)) {
+        cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "make_context: scalar must be s, d, c or z");
+        return nullptr;
+    }
+    auto* h = new cosma_gpu_mm_handle();
+    h->scalar = s;
+    h->n_streams = streams > 0 ? streams : cgb::default_streams();
+    if (h->n_streams < 1) h->n_streams = 1;
+    h->tile_m = tile_m > 0 ? tile_m : cgb::default_tile_m();
+    h->tile_n = tile_n > 0 ? tile_n : cgb::default_tile_n();
+    h->tile_k = tile_k > 0 ? tile_k : cgb::default_tile_k();
+    h->method = cgb::default_method();
+    if (cgb::handle_init(h) != COSMA_GPU_SUCCESS) {
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+void cosma_gpu_tmm_destroy_context(cosma_gpu_mm_handle* h) {
+    if (!h) return;
+    {
+        std::lock_guard<std::mutex> lock(h->mu);
+        cudaSetDevice(h->device);
+        for (auto s : h->streams) cudaStreamSynchronize(s);
+        for (auto& b : h->bufA) b.release();
+        for (auto& b : h->bufB) b.release();
+        for (auto& b : h->bufC) b.release();
+        h->full_c.release();
+        for (auto& kv : h->pinned) cudaHostUnregister((void*)kv.first);
+        h->pinned.clear();
+        for (auto s : h->streams) cudaStreamDestroy(s);
+        cudaGetLastError();
+    }
+    delete h;
+}
+
+int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* h, int method, int slices) {
+    cgb::clear_error();
+    if (!h) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "set_method: null handle");
+    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_BF16X3)
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "set_method: unknown method");
+    std::lock_guard<std::mutex> lock(h->mu);
+    h->method = method;
+    h->slices = slices;
+    return COSMA_GPU_SUCCESS;
+}
+
+void* cosma_gpu_tmm_device_buffer_c(cosma_gpu_mm_handle* h) { return h ? h->last_device_c : nullptr; }
+
+int cosma_gpu_tmm_last_ozaki_info(cosma_gpu_mm_handle* h, cosma_gpu_ozaki_info* info) {
+    if (!h || !info) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "last_ozaki_info: null argument");
+    *info = h->last_info;
+    return COSMA_GPU_SUCCESS;
+}
+
+int cosma_gpu_tmm_gemm_d(cosma_gpu_mm_handle* h, char ta, char tb, int m, int n, int k, double alpha, const double* A,
+                         int lda, const double* B, int ldb, double beta, double* C, int ldc, int pin, int copy_c_back) {
+    cgb::clear_error();
+    double a[2] = {alpha, 0}, b[2] = {beta, 0};
+    return cgb::tmm_gemm(h, cgb::Scalar::D, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc, pin != 0, copy_c_back != 0);
+}
+int cosma_gpu_tmm_gemm_s(cosma_gpu_mm_handle* h, char ta, char tb, int m, int n, int k, float alpha, const float* A,
+                         int lda, const float* B, int ldb, float beta, float* C, int ldc, int pin, int copy_c_back) {
+    cgb::clear_error();
+    double a[2] = {alpha, 0}, b[2] = {beta, 0};
+    return cgb::tmm_gemm(h, cgb::Scalar::S, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc, pin != 0, copy_c_back != 0);
+}
+int cosma_gpu_tmm_gemm_z(cosma_gpu_mm_handle* h, char ta, char tb, int m, int n, int k, const double* alpha,
+                         const double* A, int lda, const double* B, int ldb, const double* beta, double* C, int ldc,
+                         int pin, int copy_c_back) {
+    cgb::clear_error();
+    double a[2] = {alpha[0], alpha[1]}, b[2] = {beta[0], beta[1]};
+    return cgb::tmm_gemm(h, cgb::Scalar::Z, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc, pin != 0, copy_c_back != 0);
+}
+int cosma_gpu_tmm_gemm_c(cosma_gpu_mm_handle* h, char ta, char tb, int m, int n, int k, const float* alpha,
+                         const float* A, int lda, const float* B, int ldb, const float* beta, float* C, int ldc,
+                         int pin, int copy_c_back) {
+    cgb::clear_error();
+    double a[2] = {alpha[0], alpha[1]}, b[2] = {beta[0], beta[1]};
+    return cgb::tmm_gemm(h, cgb::Scalar::C, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc, pin != 0, copy_c_back != 0);
+}
+
+cosma_gpu_mm_handle* cosma_gpu_context_instance(char scalar) {
+    cgb::Scalar s;
+    if (!parse_scalar(scalar, &s)) {
+        cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "context_instance: scalar must be s, d, c or z");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(g_singleton_mu);
+    int idx = (int)s;
+    if (!g_singletons[idx]) {
+        // Lives until process exit, like the reference's singleton
+        // (src/cosma/context.cpp:155-158).
+        g_singletons[idx] = cosma_gpu_tmm_make_context(scalar, 0, 0, 0, 0);
+        g_pin_default = cgb::default_pinning();
+    }
+    return g_singletons[idx];
+}
+
+}  // extern "C"
+
+// local_multiply: 'N','N', ld = m, k, m; pins host buffers when
+// COSMA_GPU_MEMORY_PINNING is ON (default), as local_multiply.cpp:342-347.
+template <class T>
+static int local_multiply_impl(cosma_gpu_mm_handle* h, char scalar, cgb::Scalar sc, T* a, T* b, T* c, int m, int n,
+                               int k, const double* alpha, const double* beta, int copy_c_back) {
+    cgb::clear_error();
+    if (!h) h = cosma_gpu_context_instance(scalar);
+    if (!h) return cosma_gpu_last_error();
+    return cgb::tmm_gemm(h, sc, 'N', 'N', m, n, k, alpha, a, std::max(1, m), b, std::max(1, k), beta, c,
+                         std::max(1, m), g_pin_default, copy_c_back != 0);
+}
+
+extern "C" {
+
+int cosma_gpu_local_multiply_d(cosma_gpu_mm_handle* h, double* a, double* b, double* c, int m, int n, int k,
+                               double alpha, double beta, int copy_c_back) {
+    double al[2] = {alpha, 0}, be[2] = {beta, 0};
+    return local_multiply_impl(h, 'd', cgb::Scalar::D, a, b, c, m, n, k, al, be, copy_c_back);
+}
+int cosma_gpu_local_multiply_s(cosma_gpu_mm_handle* h, float* a, float* b, float* c, int m, int n, int k, float alpha,
+                               float beta, int copy_c_back) {
+    double al[2] = {alpha, 0}, be[2] = {beta, 0};
+    return local_multiply_impl(h, 's', cgb::Scalar::S, a, b, c, m, n, k, al, be, copy_c_back);
+}
+int cosma_gpu_local_multiply_z(cosma_gpu_mm_handle* h, double* a, double* b, double* c, int m, int n, int k,
+                               const double* alpha, const double* beta, int copy_c_back) {
+    double al[2] = {alpha[0], alpha[1]}, be[2] = {beta[0], beta[1]};
+    return local_multiply_impl(h, 'z', cgb::Scalar::Z, a, b, c, m, n, k, al, be, copy_c_back);
+}
+int cosma_gpu_local_multiply_c(cosma_gpu_mm_handle* h, float* a, float* b, float* c, int m, int n, int k,
+                               const float* alpha, const float* beta, int copy_c_back) {
+    double al[2] = {alpha[0], alpha[1]}, be[2] = {beta[0], beta[1]};
+    return local_multiply_impl(h, 'c', cgb::Scalar::C, a, b, c, m, n, k, al, be, copy_c_back);
+}
+
+}  // extern "C"

@@ -1,0 +1,234 @@
+/*
+ * cosma_gb300.h - C ABI of the GB300 (sm_103a) single-process GEMM path.
+ *
+ * This is the drop-in boundary for COSMA's one-rank GEMM path.  Every entry
+ * point takes plain pointers and sizes; matrices are column-major.  Pointers
+ * passed to the Tiled-MM / local_multiply / p?gemm entry points may be host
+ * or device pointers (detected with cudaPointerGetAttributes); the *_device
+ * entry points take device pointers and a cudaStream_t passed as void*.
+ *
+ * Complex scalars are passed as pointers to two consecutive reals (re, im),
+ * exactly as the reference's ScaLAPACK ABI does (src/cosma/pxgemm.h:16-26).
+ *
+ * Errors: entry points that return int return COSMA_GPU_SUCCESS (0) or one
+ * of the codes below and record a message for cosma_gpu_last_error_string().
+ * The reference throws std::runtime_error on GPU errors
+ * (src/cosma/gpu/utils.hpp:7-13); the ScaLAPACK entry points here are void
+ * like the reference's, so their status is read via cosma_gpu_last_error().
+ */
+#ifndef COSMA_GB300_H
+#define COSMA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define COSMA_GPU_SUCCESS 0
+#define COSMA_GPU_ERROR_INVALID_ARGUMENT 1
+#define COSMA_GPU_ERROR_CUDA 2
+#define COSMA_GPU_ERROR_OUT_OF_MEMORY 3
+#define COSMA_GPU_ERROR_NOT_SUPPORTED 4
+#define COSMA_GPU_ERROR_DEVICE_TIMEOUT 5
+#define COSMA_GPU_ERROR_INTERNAL 6
+
+/* Status of the last failing call on this thread (0 if none since the last
+ * successful call). */
+int cosma_gpu_last_error(void);
+const char* cosma_gpu_last_error_string(void);
+/* Library version string. */
+const char* cosma_gpu_version(void);
+
+/* ------------------------------------------------------ arithmetic methods */
+/* NATIVE: FP64 (complex FP64) arithmetic on the FP64 tensor path.
+ * OZAKI : FP64-accurate GEMM from integer slices (|digit| <= 16) multiplied
+ *         exactly on the FP8 tensor cores with FP32 accumulation, recombined
+ *         in FP64 (real double / complex double only).
+ * BF16X3: single precision from three BF16 slices per operand, six slice
+ *         products accumulated in FP32 on the BF16 tensor cores (float only).
+ * AUTO  : NATIVE for every type (the reference's semantics). */
+#define COSMA_GPU_METHOD_AUTO 0
+#define COSMA_GPU_METHOD_NATIVE 1
+#define COSMA_GPU_METHOD_OZAKI 2
+#define COSMA_GPU_METHOD_BF16X3 3
+
+/* Statistics of one Ozaki-split GEMM (filled when a non-null pointer is
+ * given). */
+typedef struct cosma_gpu_ozaki_info {
+    int slices;          /* digits per operand element                      */
+    int products;        /* slice-pair GEMMs executed                       */
+    int groups;          /* FP32 accumulator drains per output tile         */
+    int fallback_native; /* 1 if non-finite input forced the native path    */
+    double spread_bits;  /* exponent-spread estimate used to size slices    */
+} cosma_gpu_ozaki_info;
+
+/* ----------------------------------------------------- Tiled-MM interface */
+/* Replaces gpu::make_context<T>(streams, tile_m, tile_n, tile_k)
+ * (called at src/cosma/context.cpp:24-25,45; Tiled-MM v2.3.2).
+ * scalar: 's', 'd', 'c' or 'z'.  Non-positive sizes select the defaults
+ * (COSMA_GPU_STREAMS / COSMA_GPU_MAX_TILE_{M,N,K} or the built-in values). */
+typedef struct cosma_gpu_mm_handle cosma_gpu_mm_handle;
+cosma_gpu_mm_handle* cosma_gpu_tmm_make_context(char scalar, int streams, int tile_m,
+                                                int tile_n, int tile_k);
+void cosma_gpu_tmm_destroy_context(cosma_gpu_mm_handle* handle);
+/* Selects the arithmetic used by the handle's gemm calls.  ozaki_slices <= 0
+ * lets the library size the slices from the inputs. */
+int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* handle, int method, int ozaki_slices);
+/* Device buffer holding the C of the last call made with copy_c_back == 0
+ * (replaces mm_handle::get_full_device_buffer_c(), src/cosma/gpu/nccl_utils.cpp:200). */
+void* cosma_gpu_tmm_device_buffer_c(cosma_gpu_mm_handle* handle);
+/* Ozaki statistics of the handle's last call. */
+int cosma_gpu_tmm_last_ozaki_info(cosma_gpu_mm_handle* handle, cosma_gpu_ozaki_info* info);
+
+/* Replaces gpu::gemm(mm_handle<T>&, transa, transb, m, n, k, alpha, A, lda,
+ * B, ldb, beta, C, ldc, pin_host_buffers, copy_c_back)
+ * (call site src/cosma/local_multiply.cpp:245-260; Tiled-MM v2.3.2).
+ * C = alpha * op(A) * op(B) + beta * C, op in {'N','T','C'} (case-insensitive).
+ * With beta == 0, C is never read (it may hold NaN). */
+int cosma_gpu_tmm_gemm_s(cosma_gpu_mm_handle* h, char transa, char transb, int m, int n, int k,
+                         float alpha, const float* A, int lda, const float* B, int ldb,
+                         float beta, float* C, int ldc, int pin_host_buffers, int copy_c_back);
+int cosma_gpu_tmm_gemm_d(cosma_gpu_mm_handle* h, char transa, char transb, int m, int n, int k,
+                         double alpha, const double* A, int lda, const double* B, int ldb,
+                         double beta, double* C, int ldc, int pin_host_buffers, int copy_c_back);
+int cosma_gpu_tmm_gemm_c(cosma_gpu_mm_handle* h, char transa, char transb, int m, int n, int k,
+                         const float* alpha, const float* A, int lda, const float* B, int ldb,
+                         const float* beta, float* C, int ldc, int pin_host_buffers,
+                         int copy_c_back);
+int cosma_gpu_tmm_gemm_z(cosma_gpu_mm_handle* h, char transa, char transb, int m, int n, int k,
+                         const double* alpha, const double* A, int lda, const double* B,
+                         int ldb, const double* beta, double* C, int ldc,
+                         int pin_host_buffers, int copy_c_back);
+
+/* --------------------------------------------------- COSMA local_multiply */
+/* Replaces cosma::local_multiply(cosma_context<T>*, a, b, c, m, n, k, alpha,
+ * beta, copy_c_back) (src/cosma/local_multiply.hpp:6-16,
+ * src/cosma/local_multiply.cpp:300-381) and, with handle == NULL, the
+ * context-less overload (src/cosma/local_multiply.hpp:40-49) that uses the
+ * per-type singleton (src/cosma/context.cpp:155-158).  A is m x k (ld m),
+ * B is k x n (ld k), C is m x n (ld m), no transposes: at P = 1
+ * cosma::multiply reduces to exactly this call (src/cosma/multiply.cpp:369-394). */
+int cosma_gpu_local_multiply_s(cosma_gpu_mm_handle* h, float* a, float* b, float* c, int m,
+                               int n, int k, float alpha, float beta, int copy_c_back);
+int cosma_gpu_local_multiply_d(cosma_gpu_mm_handle* h, double* a, double* b, double* c, int m,
+                               int n, int k, double alpha, double beta, int copy_c_back);
+int cosma_gpu_local_multiply_c(cosma_gpu_mm_handle* h, float* a, float* b, float* c, int m,
+                               int n, int k, const float* alpha, const float* beta,
+                               int copy_c_back);
+int cosma_gpu_local_multiply_z(cosma_gpu_mm_handle* h, double* a, double* b, double* c, int m,
+                               int n, int k, const double* alpha, const double* beta,
+                               int copy_c_back);
+/* The per-type singleton context (replaces get_context_instance<T>(),
+ * src/cosma/context.cpp:155-158).  Owned by the library. */
+cosma_gpu_mm_handle* cosma_gpu_context_instance(char scalar);
+
+/* -------------------------------------------------- device-pointer GEMMs */
+/* Stream-ordered GEMM on device pointers: no host synchronisation, no copies.
+ * 64-bit sizes (the reference's int products m*k overflow at 65536^2,
+ * src/cosma/local_multiply.cpp:343-346). */
+int cosma_gpu_dgemm_device(int method, char transa, char transb, int64_t m, int64_t n,
+                           int64_t k, double alpha, const double* A, int64_t lda,
+                           const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                           void* stream);
+int cosma_gpu_zgemm_device(int method, char transa, char transb, int64_t m, int64_t n,
+                           int64_t k, const double* alpha, const double* A, int64_t lda,
+                           const double* B, int64_t ldb, const double* beta, double* C,
+                           int64_t ldc, void* stream);
+int cosma_gpu_sgemm_device(int method, char transa, char transb, int64_t m, int64_t n,
+                           int64_t k, float alpha, const float* A, int64_t lda,
+                           const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                           void* stream);
+int cosma_gpu_cgemm_device(int method, char transa, char transb, int64_t m, int64_t n,
+                           int64_t k, const float* alpha, const float* A, int64_t lda,
+                           const float* B, int64_t ldb, const float* beta, float* C,
+                           int64_t ldc, void* stream);
+/* FP64-accurate Ozaki-split DGEMM (no counterpart in the reference, which
+ * runs native DGEMM).  slices <= 0 sizes the slice count from the inputs'
+ * exponent spread; `info` may be NULL. */
+int cosma_gpu_dgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                 double alpha, const double* A, int64_t lda, const double* B,
+                                 int64_t ldb, double beta, double* C, int64_t ldc, int slices,
+                                 void* stream, cosma_gpu_ozaki_info* info);
+
+/* ------------------------------------- COSTA 1x1-grid layout transforms */
+/* dst(rows x cols) = op(src) where op in {'N','T','C'}: the block-cyclic ->
+ * COSMA-blocked pack that costa::transformer::schedule(scalapack -> cosma,
+ * trans, 1, 0) + transform() performs on one rank
+ * (src/cosma/cosma_pxgemm.cpp:338-343).  Bit-exact copy.  elem_bytes is 4
+ * (s), 8 (d or c) or 16 (z); conjugation flips the sign bit of imaginary
+ * parts (elem_bytes 8 with is_complex=1 means complex float). */
+int costa_gpu_pack(char op, int is_complex, int elem_bytes, int64_t rows, int64_t cols,
+                   const void* src, int64_t ld_src, void* dst, int64_t ld_dst, void* stream);
+/* dst = alpha * src + beta * dst (dst is not read when beta == 0): the
+ * COSMA -> ScaLAPACK back-transform of C with alpha/beta
+ * (src/cosma/cosma_pxgemm.cpp:362-364).  Real: products rounded as
+ * fl(fl(alpha*s) + fl(beta*d)) without contraction. */
+int costa_gpu_unpack_d(int64_t rows, int64_t cols, double alpha, const double* src,
+                       int64_t ld_src, double beta, double* dst, int64_t ld_dst, void* stream);
+int costa_gpu_unpack_z(int64_t rows, int64_t cols, const double* alpha, const double* src,
+                       int64_t ld_src, const double* beta, double* dst, int64_t ld_dst,
+                       void* stream);
+int costa_gpu_unpack_s(int64_t rows, int64_t cols, float alpha, const float* src,
+                       int64_t ld_src, float beta, float* dst, int64_t ld_dst, void* stream);
+int costa_gpu_unpack_c(int64_t rows, int64_t cols, const float* alpha, const float* src,
+                       int64_t ld_src, const float* beta, float* dst, int64_t ld_dst,
+                       void* stream);
+
+/* ------------------------------------------- ScaLAPACK p?gemm (1x1 grid) */
+/* Replace the reference's interposed ScaLAPACK symbols (src/cosma/pxgemm.h:6-107,
+ * src/cosma/pxgemm.cpp:8-...) and the prefixed cosma_p?gemm family
+ * (src/cosma/prefixed_pxgemm.h:6-54).  Only a 1x1 process grid is accepted:
+ * if BLACS' Cblacs_gridinfo is linked it is asked for the grid, otherwise the
+ * grid is taken to be 1x1.  Descriptors: desc[1] ctxt, desc[2..3] M,N,
+ * desc[4..5] MB,NB, desc[6..7] RSRC,CSRC, desc[8] LLD (src/cosma/scalapack.hpp:11-47). */
+#define COSMA_GPU_PXGEMM_ARGS(T)                                                              \
+    const char *transa, const char *transb, const int *m, const int *n, const int *k,        \
+        const T *alpha, const T *a, const int *ia, const int *ja, const int *desca,          \
+        const T *b, const int *ib, const int *jb, const int *descb, const T *beta, T *c,     \
+        const int *ic, const int *jc, const int *descc
+
+void psgemm(COSMA_GPU_PXGEMM_ARGS(float));
+void pdgemm(COSMA_GPU_PXGEMM_ARGS(double));
+void pcgemm(COSMA_GPU_PXGEMM_ARGS(float));
+void pzgemm(COSMA_GPU_PXGEMM_ARGS(double));
+void psgemm_(COSMA_GPU_PXGEMM_ARGS(float));
+void pdgemm_(COSMA_GPU_PXGEMM_ARGS(double));
+void pcgemm_(COSMA_GPU_PXGEMM_ARGS(float));
+void pzgemm_(COSMA_GPU_PXGEMM_ARGS(double));
+void PSGEMM(COSMA_GPU_PXGEMM_ARGS(float));
+void PDGEMM(COSMA_GPU_PXGEMM_ARGS(double));
+void PCGEMM(COSMA_GPU_PXGEMM_ARGS(float));
+void PZGEMM(COSMA_GPU_PXGEMM_ARGS(double));
+void PSGEMM_(COSMA_GPU_PXGEMM_ARGS(float));
+void PDGEMM_(COSMA_GPU_PXGEMM_ARGS(double));
+void PCGEMM_(COSMA_GPU_PXGEMM_ARGS(float));
+void PZGEMM_(COSMA_GPU_PXGEMM_ARGS(double));
+void cosma_psgemm(COSMA_GPU_PXGEMM_ARGS(float));
+void cosma_pdgemm(COSMA_GPU_PXGEMM_ARGS(double));
+void cosma_pcgemm(COSMA_GPU_PXGEMM_ARGS(float));
+void cosma_pzgemm(COSMA_GPU_PXGEMM_ARGS(double));
+void cosma_psgemm_(COSMA_GPU_PXGEMM_ARGS(float));
+void cosma_pdgemm_(COSMA_GPU_PXGEMM_ARGS(double));
+void cosma_pcgemm_(COSMA_GPU_PXGEMM_ARGS(float));
+void cosma_pzgemm_(COSMA_GPU_PXGEMM_ARGS(double));
+void COSMA_PSGEMM(COSMA_GPU_PXGEMM_ARGS(float));
+void COSMA_PDGEMM(COSMA_GPU_PXGEMM_ARGS(double));
+void COSMA_PCGEMM(COSMA_GPU_PXGEMM_ARGS(float));
+void COSMA_PZGEMM(COSMA_GPU_PXGEMM_ARGS(double));
+void COSMA_PSGEMM_(COSMA_GPU_PXGEMM_ARGS(float));
+void COSMA_PDGEMM_(COSMA_GPU_PXGEMM_ARGS(double));
+void COSMA_PCGEMM_(COSMA_GPU_PXGEMM_ARGS(float));
+void COSMA_PZGEMM_(COSMA_GPU_PXGEMM_ARGS(double));
+
+/* Method used by the p?gemm entry points (default NATIVE; the
+ * COSMA_GPU_GEMM_METHOD environment variable "native"/"ozaki"/"bf16x3"
+ * sets the initial value). */
+int cosma_gpu_pxgemm_set_method(int method);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COSMA_GB300_H */

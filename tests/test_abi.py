@@ -1,0 +1,55 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares (CPU)."""
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"#define[^\n]*(\\\n[^\n]*)*", "", text)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text):
+            name = m.group(1)
+            if name in {"if", "for", "while", "return", "sizeof", "COSMA_GPU_PXGEMM_ARGS"}:
+                continue
+            # function declarations end with ');' after the parameter list
+            tail = text[m.end():]
+            depth, i = 1, 0
+            while depth and i < len(tail):
+                depth += {"(": 1, ")": -1}.get(tail[i], 0)
+                i += 1
+            if tail[i:].lstrip().startswith(";"):
+                names.add(name)
+    return names
+
+
+def test_header_declares_the_drop_in_surface():
+    names = declared_symbols()
+    for must in ["pdgemm_", "pzgemm_", "psgemm", "PDGEMM_", "cosma_pdgemm", "COSMA_PZGEMM_",
+                 "cosma_gpu_tmm_gemm_d", "cosma_gpu_tmm_make_context", "cosma_gpu_local_multiply_d",
+                 "cosma_gpu_dgemm_ozaki_device", "costa_gpu_pack", "costa_gpu_unpack_d"]:
+        assert must in names, must
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    names = declared_symbols()
+    assert len(names) >= 60
+    missing = [n for n in sorted(names) if not hasattr(native_lib, n)]
+    assert not missing, missing
+
+
+def test_build_targets_sm_103a_only():
+    from cosma_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_version_string_without_gpu(native_lib):
+    assert b"sm_103a" in native_lib.cosma_gpu_version()
+
+
+def test_python_bindings_cover_the_header():
+    from cosma_gb300 import _native
+    assert declared_symbols() <= set(_native.SIGNATURES)

@@ -1,0 +1,120 @@
+"""ScaLAPACK p?gemm on a 1x1 grid vs the oracle: the reference's 1x1 test
+cases (tests/pdgemm.cpp:382-383,415,419-456,796-907) and its edge cases,
+checked with its validate_results (utils/pxgemm_utils.hpp:415-449, 1e-6)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_case(ma, na, mb_, nb_, mc, nc, bma, bna, bmb, bnb, bmc, bnc, ia, ja, ib, jb, ic, jc, m, n, k, ta, tb,
+              alpha, beta, lld_a, lld_b, lld_c, seed=0, dtype=np.float64, prefix="p", suffix="_", method=None):
+    from cosma_gb300 import descinit, pxgemm, pxgemm_set_method
+    rng_seed = seed * 7919 + m * 31 + n * 17 + k
+    A = oracle.uniform((lld_a, na), rng_seed + 1, 0.0, 1.0, dtype=dtype)  # random_generator: U[0, 1)
+    B = oracle.uniform((lld_b, nb_), rng_seed + 2, 0.0, 1.0, dtype=dtype)
+    C = oracle.uniform((lld_c, nc), rng_seed + 3, 0.0, 1.0, dtype=dtype)
+    if beta == 0:  # pdgemm must not read C when beta == 0 (pxgemm_utils.hpp:604-614)
+        C[ic - 1:ic - 1 + m, jc - 1:jc - 1 + n] = np.nan
+    desca = descinit(ma, na, bma, bna, 0, 0, 0, lld_a)
+    descb = descinit(mb_, nb_, bmb, bnb, 0, 0, 0, lld_b)
+    descc = descinit(mc, nc, bmc, bnc, 0, 0, 0, lld_c)
+    # oracle: COSTA pack -> gemm NN (alpha 1, beta 0) -> unpack alpha/beta
+    Asub = A[ia - 1:ia - 1 + (m if ta == "N" else k), ja - 1:ja - 1 + (k if ta == "N" else m)]
+    Bsub = B[ib - 1:ib - 1 + (k if tb == "N" else n), jb - 1:jb - 1 + (n if tb == "N" else k)]
+    Ap = oracle.pack(ta, np.asfortranarray(Asub), m, k)
+    Bp = oracle.pack(tb, np.asfortranarray(Bsub), k, n)
+    Cc = oracle.gemm("N", "N", 1.0, Ap, Bp, 0.0, np.zeros((m, n), dtype=dtype, order="F"))
+    ref = C.copy(order="F")
+    sub = np.asfortranarray(ref[ic - 1:ic - 1 + m, jc - 1:jc - 1 + n])
+    if k == 0 or alpha == 0:
+        sub = oracle.scale(beta, sub) if beta != 0 else np.zeros_like(sub)
+    else:
+        oracle.unpack(alpha, Cc, beta, sub)
+    ref[ic - 1:ic - 1 + m, jc - 1:jc - 1 + n] = sub
+    if method:
+        pxgemm_set_method(method)
+    try:
+        pxgemm(ta, tb, m, n, k, alpha, A, ia, ja, desca, B, ib, jb, descb, beta, C, ic, jc, descc, prefix=prefix,
+               suffix=suffix)
+    finally:
+        if method:
+            pxgemm_set_method("native")
+    got = C
+    assert oracle.validate_results(got[ic - 1:ic - 1 + m, jc - 1:jc - 1 + n], ref[ic - 1:ic - 1 + m, jc - 1:jc - 1 + n])
+    # everything outside the C sub-matrix is untouched (bit for bit)
+    mask = np.ones(got.shape, bool)
+    mask[ic - 1:ic - 1 + m, jc - 1:jc - 1 + n] = False
+    assert got[mask].tobytes() == ref[mask].tobytes()
+
+
+def _short(m, n, k, bm, bn, bk, ta, tb, alpha, beta, **kw):
+    """pxgemm_params short constructor (src/cosma/pxgemm_params.hpp:177-200) on a 1x1 grid."""
+    bma, bna = (bk, bm) if ta != "N" else (bm, bk)
+    bmb, bnb = (bn, bk) if tb != "N" else (bk, bn)
+    ma, na = (k, m) if ta != "N" else (m, k)
+    mb_, nb_ = (n, k) if tb != "N" else (k, n)
+    _run_case(ma, na, mb_, nb_, m, n, bma, bna, bmb, bnb, bm, bn, 1, 1, 1, 1, 1, 1, m, n, k, ta, tb, alpha, beta,
+              max(1, ma), max(1, mb_), max(1, m), **kw)
+
+
+@pytest.mark.parametrize("case", [
+    (10, 10, 10, 2, 2, 2, "N", "N", 1.0, 0.0),   # tests/pdgemm.cpp:382
+    (10, 11, 13, 2, 2, 2, "N", "N", 1.0, 0.0),   # tests/pdgemm.cpp:383
+    (3, 3, 7, 3, 3, 3, "T", "N", 1.0, 0.0),      # tests/pdgemm.cpp:415
+    (10, 11, 12, 3, 2, 3, "T", "N", 1.0, 1.0),   # alpha/beta variants (tests/pdgemm.cpp:392-404)
+    (10, 11, 12, 3, 2, 3, "T", "N", 0.0, 0.0),
+    (10, 11, 12, 3, 2, 3, "T", "N", 0.0, 1.0),
+    (10, 11, 12, 3, 2, 3, "T", "N", 0.5, 0.5),
+    (5, 5, 5, 2, 2, 2, "T", "N", 0.5, 0.0),
+    (8, 4, 8, 2, 2, 2, "N", "N", 0.5, 0.0),
+    (13, 13, 448, 13, 13, 13, "N", "N", 1.0, 0.5),
+    (26, 13, 448, 13, 13, 13, "T", "N", 1.0, 0.5),
+])
+def test_reference_one_by_one_cases(native_lib, cuda, case):
+    _short(*case)
+
+
+def test_adapt_strategy_case(native_lib, cuda):
+    # tests/pdgemm.cpp:419-456: A 1280x128 'T', bs 32, m = n = 128, k = 1280, 1x1 'C'
+    _run_case(1280, 128, 1280, 128, 128, 128, 32, 32, 32, 32, 32, 32, 1, 1, 1, 1, 1, 1, 128, 128, 1280, "T", "N",
+              1.0, 0.0, 1280, 1280, 128)
+
+
+@pytest.mark.parametrize("ta,tb,nn", [("N", "T", 83), ("T", "N", 77)])
+def test_83_cases(native_lib, cuda, ta, tb, nn):
+    # tests/pdgemm.cpp:796-907 (problem sizes :813, :850, :887)
+    _run_case(83, 83, 83, nn, 83, nn, 32, 32, 32, 32, 32, 32, 1, 1, 1, 1, 1, 1, 83, nn, 83, ta, tb, 1.0, 0.0, 83, 83, 83)
+
+
+def test_submatrix_offsets_and_padding(native_lib, cuda):
+    # sub-matrices ia, ja, ib, jb, ic, jc != 1 with LLD > M on a 1x1 grid
+    _run_case(40, 50, 60, 45, 30, 35, 8, 8, 8, 8, 8, 8, 3, 5, 7, 2, 4, 6, 20, 25, 30, "N", "N", 1.5, 0.5, 47, 61, 33)
+    _run_case(50, 40, 45, 60, 30, 35, 8, 8, 8, 8, 8, 8, 5, 3, 2, 7, 4, 6, 20, 25, 30, "T", "T", -1.0, 2.0, 50, 45, 30)
+
+
+@pytest.mark.parametrize("m,n,k", [(0, 5, 5), (5, 0, 5), (5, 5, 0)])
+def test_zero_sizes(native_lib, cuda, m, n, k):
+    # m or n == 0: no-op; k == 0: C <- beta*C (cosma_pxgemm.cpp:39-46)
+    _run_case(max(m, 1), max(k, 1), max(k, 1), max(n, 1), max(m, 1), max(n, 1), 2, 2, 2, 2, 2, 2, 1, 1, 1, 1, 1, 1,
+              m, n, k, "N", "N", 1.0, 0.5, max(m, 1), max(k, 1), max(m, 1))
+
+
+def test_lowercase_flags_and_all_spellings(native_lib, cuda):
+    for prefix, suffix in [("p", ""), ("p", "_"), ("P", ""), ("P", "_"), ("cosma_p", ""), ("cosma_p", "_"),
+                           ("COSMA_P", ""), ("COSMA_P", "_")]:
+        _run_case(9, 7, 7, 8, 9, 8, 2, 2, 2, 2, 2, 2, 1, 1, 1, 1, 1, 1, 9, 8, 7, "n", "n", 1.0, 0.0, 9, 7, 9,
+                  prefix=prefix, suffix=suffix)
+
+
+def test_pzgemm_conjugate(native_lib, cuda):
+    _run_case(12, 10, 12, 11, 10, 11, 4, 4, 4, 4, 4, 4, 1, 1, 1, 1, 1, 1, 10, 11, 12, "C", "N", 1.0 - 1.0j,
+              0.5 + 0.5j, 12, 12, 10, dtype=np.complex128)
+
+
+def test_psgemm(native_lib, cuda):
+    # FP32: validate_results 1e-6 relative to max(1e-3, |v|) at k = 40
+    _run_case(30, 40, 40, 20, 30, 20, 8, 8, 8, 8, 8, 8, 1, 1, 1, 1, 1, 1, 30, 20, 40, "N", "N", 1.0, 0.0, 30, 40, 30,
+              dtype=np.float32)
