@@ -1,0 +1,338 @@
+#!/usr/bin/env python3
+"""Benchmark of the one-rank GEMM path on GB300.
+
+Workload (the precision configuration): C = A*B with m = n = k = 16384, FP64,
+column-major, entries u*2^e (u ~ U[-1, 1], integer e ~ U{-phi..phi}, phi = 0
+for the headline, 8 and 32 as variants), seeded synthetic data.  One step is
+one FP64-accurate GEMM through the Ozaki-split path (integer slices on the
+FP8 tensor cores, exact accumulation, FP64 recombination) with the inputs
+resident in HBM; `e2e` runs the same GEMM through the Tiled-MM C-ABI entry
+point (cosma_gpu_tmm_gemm_d) from pinned host buffers, copies included.
+Beside it: the native FP64 (DMMA) kernel on the same inputs, the accuracy of
+both against a double-double oracle on sampled entries, the roofline of the
+dominant kernel, and the reference's CPU path (OpenBLAS DGEMM, the arithmetic
+cblas_dgemm performs at P = 1) timed on the host cores.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "FP64-accurate GEMM TFLOP/s: INT8-split vs native FP64 at <=1e-15 rel err"
+UNIT = "TFLOP/s"
+KERNELS_PER_STEP = 6  # A scale (2), B scale (1), A split, B split, slice-product GEMM
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--size", type=int, default=16384)
+    p.add_argument("--phi", type=int, default=0)
+    p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison run")
+    p.add_argument("--no-variants", action="store_true", help="skip the phi = 8 / 32 variants")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config(n, phi):
+    return {"workload": f"precision: FP64-accurate DGEMM NN m=n=k={n}, u*2^e entries phi={phi}",
+            "m": n, "n": n, "k": n, "phi": phi, "layout": "column-major", "alpha": 1.0, "beta": 0.0,
+            "l2": "inputs larger than L2 (2 GiB per operand vs 129 MB)", "parallelism": "replicas"}
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        under = sorted(sm)[len(sm) // 4:] if sm else []  # drop idle edges of the window
+        return {"sm_mhz": float(np.median(under)) if under else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_dgemm_sample(A, B, budget_s=12.0):
+    """OpenBLAS DGEMM (numpy) on a K-slab of the workload, sized to ~budget_s."""
+    n = A.shape[0]
+    kb = 512
+    t = time.perf_counter()
+    np.matmul(A[:, :kb], B[:kb, :])
+    dt = time.perf_counter() - t
+    rate = 2.0 * n * n * kb / max(dt, 1e-6)
+    kb = int(min(A.shape[1], max(512, (budget_s * rate) / (2.0 * n * n))))
+    kb -= kb % 256
+    t = time.perf_counter()
+    np.matmul(A[:, :kb], B[:kb, :])
+    dt = time.perf_counter() - t
+    return 2.0 * n * n * kb / dt / 1e12, kb, dt
+
+
+def run_reference(args):
+    """The reference's CPU path on the host cores: at P = 1 cosma::multiply is
+    one cblas_dgemm(ColMajor, N, N) (src/cosma/blas.cpp:35-48); the reference
+    cannot be built here (MPI, ScaLAPACK, COSTA and Tiled-MM are absent), so
+    its arithmetic runs through numpy's OpenBLAS on every host thread."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    n = args.size
+    A = oracle.exp_spread((n, n), 1, args.phi)
+    B = oracle.exp_spread((n, n), 2, args.phi)
+    kb = 1024
+    for _ in range(max(1, args.warmup)):
+        np.matmul(A[:, :kb], B[:kb, :])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        np.matmul(A[:, :kb], B[:kb, :])
+    dt = time.perf_counter() - t0
+    flops = 2.0 * n * n * kb * args.steps
+    val = flops / dt / 1e12
+    cores = int(os.environ.get("OPENBLAS_NUM_THREADS", os.cpu_count() or 1))
+    out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": config(n, args.phi),
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"OpenBLAS DGEMM NN {n}x{n}x{kb} K-slab of the workload per step"},
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+
+    import cosma_gb300 as cg
+    import oracle
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    cg.load()
+    n, phi = args.size, args.phi
+    A = oracle.exp_spread((n, n), 1 + 10 * rank, phi)
+    B = oracle.exp_spread((n, n), 2 + 10 * rank, phi)
+    dA = torch.from_numpy(A.reshape(-1, order="F")).to(dev)
+    dB = torch.from_numpy(B.reshape(-1, order="F")).to(dev)
+    dC = torch.empty(n * n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        return cg.dgemm_ozaki_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, stream=stream)
+
+    for _ in range(max(args.warmup, 3)):
+        info = step()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    gemm_ms = []
+    for _ in range(args.steps):
+        info = step()
+        gemm_ms.append(info["gemm_ms"])
+    ev1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    flops = 2.0 * n * n * n
+    value = flops * world / (ms * 1e-3) / 1e12
+
+    # accuracy against the double-double oracle on sampled entries
+    rng = np.random.default_rng(1234)
+    ns = 4096
+    rows, cols = rng.integers(0, n, ns), rng.integers(0, n, ns)
+    Cg = dC.cpu().numpy().reshape(n, n).T  # column-major view
+    hi, lo, ab = oracle.gemm_dd_sampled("N", "N", A, B, rows, cols)
+    acc = oracle.error_stats(Cg[rows, cols], hi, lo, ab)
+
+    # native FP64 on the same inputs (one run)
+    native = None
+    if not args.no_native:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cg.gemm_device("N", "N", n, n, 256, 1.0, dA, n, dB, n, 0.0, dC, n, method="native", stream=stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        cg.gemm_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, method="native", stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        nms = e0.elapsed_time(e1)
+        Cn = dC.cpu().numpy().reshape(n, n).T
+        native = {"tflops": flops / (nms * 1e-3) / 1e12, "ms": nms,
+                  "accuracy": oracle.error_stats(Cn[rows, cols], hi, lo, ab)}
+
+    # end to end through the Tiled-MM C-ABI entry point, pinned host buffers
+    hA = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hB = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hC = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+    hA.numpy()[:] = A.reshape(-1, order="F")
+    hB.numpy()[:] = B.reshape(-1, order="F")
+    del dA, dB, dC
+    torch.cuda.empty_cache()
+    h = cg.make_context("d", 2, 0, 0, 0)
+    h.set_method("ozaki", 0)
+    cg.gemm(h, "N", "N", n, n, n, 1.0, hA, n, hB, n, 0.0, hC, n)  # warm-up (allocates tile buffers)
+    barrier()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        cg.gemm(h, "N", "N", n, n, n, 1.0, hA, n, hB, n, 0.0, hC, n)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = flops * world / e2e_s / 1e12
+    h.close()
+
+    # exponent-spread variants (one step each)
+    variants = []
+    if not args.no_variants:
+        for vphi in (8, 32):
+            Av = oracle.exp_spread((n, n), 101 + vphi, vphi)
+            Bv = oracle.exp_spread((n, n), 202 + vphi, vphi)
+            dA = torch.from_numpy(Av.reshape(-1, order="F")).to(dev)
+            dB = torch.from_numpy(Bv.reshape(-1, order="F")).to(dev)
+            dC = torch.empty(n * n, dtype=torch.float64, device=dev)
+            cg.dgemm_ozaki_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, stream=stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            vinfo = cg.dgemm_ozaki_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            vms = e0.elapsed_time(e1)
+            Cv = dC.cpu().numpy().reshape(n, n).T
+            vhi, vlo, vab = oracle.gemm_dd_sampled("N", "N", Av, Bv, rows, cols)
+            variants.append({"phi": vphi, "tflops": flops / (vms * 1e-3) / 1e12, "slices": vinfo["slices"],
+                             "products": vinfo["products"], "spread_bits": vinfo["spread_bits"],
+                             "accuracy": oracle.error_stats(Cv[rows, cols], vhi, vlo, vab)})
+            del dA, dB, dC
+            torch.cuda.empty_cache()
+
+    # roofline of the dominant kernel (slice-product GEMM on the FP8 tensor pipe)
+    pk, pk_kind = peaks()
+    fp8_peak = 2.0 * pk["bf16_tflops"]
+    kms = float(np.median(gemm_ms))
+    achieved = info["products"] * flops / (kms * 1e-3) / 1e12
+    traffic = None
+    tf = ROOT / "profiles" / "ozaki_gemm_traffic.json"
+    if tf.exists():
+        try:
+            t = json.loads(tf.read_text())
+            traffic = t.get("bytes_per_launch_full_size")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp8_peak, "traffic": traffic,
+                "kernel": "ozaki_gemm_kernel (tcgen05 kind::f8f6f4)",
+                "peak_note": f"FP8 dense peak taken as 2x the {pk_kind} BF16 burst figure "
+                             f"({pk['bf16_tflops']} TFLOP/s)",
+                "kernel_ms": kms, "prep_ms": info["prep_ms"]}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded u*2^e)", "config": config(n, phi),
+           "ozaki": {"slices": info["slices"], "products": info["products"], "groups": info["groups"],
+                     "spread_bits": info["spread_bits"], "accuracy": acc,
+                     "accuracy_note": "4096 sampled entries vs double-double; max_rel_err is elementwise "
+                                      "|C-C_dd|/|C_dd|, max_err_over_absab normalises by (|A||B|)_ij"},
+           "native_fp64": native,
+           "speedup_vs_native": (value / world / native["tflops"]) if native else None,
+           "variants": variants, "roofline": roofline, "clocks": clocks,
+           "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
+                   "entry": "cosma_gpu_tmm_gemm_d (Tiled-MM gpu::gemm drop-in), pinned host A/B/C",
+                   "ms_per_step": e2e_s * 1e3},
+           "gpu_launches": KERNELS_PER_STEP * args.steps}
+    if rank == 0:
+        tflops_cpu, kb, cdt = cpu_dgemm_sample(A, B)
+        out["cpu_baseline"] = {"value": tflops_cpu, "unit": UNIT,
+                               "cores": int(os.environ.get("OPENBLAS_NUM_THREADS", os.cpu_count() or 1)),
+                               "kind": "port",
+                               "sample": f"OpenBLAS DGEMM NN {n}x{n}x{kb} K-slab of the workload ({cdt:.1f} s)"}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -24,7 +24,7 @@ class CosmaGpuError(RuntimeError):
 
 class OzakiInfo(C.Structure):
     _fields_ = [("slices", C.c_int), ("products", C.c_int), ("groups", C.c_int), ("fallback_native", C.c_int),
-                ("spread_bits", C.c_double)]
+                ("spread_bits", C.c_double), ("prep_ms", C.c_double), ("gemm_ms", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

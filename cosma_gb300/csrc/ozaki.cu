@@ -1,9 +1,767 @@
-// FP64-accurate Ozaki-split GEMM (placeholder until the tcgen05 kernels land).
+// FP64-accurate GEMM by Ozaki-style splitting on the FP8 tensor cores.
+//
+// The reference runs a native DGEMM (cuBLAS through Tiled-MM); this is the
+// precision form of the same operation, C = alpha*op(A)*op(B) + beta*C.
+//
+// Method (error-free splitting after Ozaki, Ogita, Oishi & Rump 2012, in the
+// integer-slice form of Ootomo, Ozaki & Yokota 2024):
+//  1. Row scaling.  Row i of op(A) gets sigma_i = 2^E_i with E_i = 1 +
+//     floor(log2 max_l |a_il|), so a'_il = a_il / sigma_i lies in (-1, 1);
+//     column j of op(B) likewise (exponent F_j).  The same pass sums
+//     2^(floor(log2|a|) - max) per row, a measure of how spread the row's
+//     exponents are, used to size the slice count.
+//  2. Slicing.  a' is rounded to F = 4 + 5(S-1) fraction bits and written
+//     as S balanced digits: a' ~= sum_s d_s 2^(-4-5(s-1)), |d_s| <= 16, the
+//     digits of |a'| in balanced base 32 (each in [-16, 15], the leading one
+//     in [0, 16]) with the sign applied to all.  Integers up to 16 are exact
+//     in FP8 E4M3, so each slice is an E4M3 matrix, stored K-major.
+//  3. Slice products.  A_s * B_t is computed exactly on the FP8 tensor cores
+//     (tcgen05 kind::f8f6f4): every product of digits is an integer of
+//     magnitude <= 256 and the FP32 accumulator holds integers up to 2^24
+//     exactly, so up to 65536/k same-weight products share one accumulator.
+//     Products with s + t > S + 1 are below the working precision and are
+//     skipped (S(S+1)/2 products).
+//  4. Recombination.  Each accumulator drain is converted to an integer and
+//     added, shifted to its weight, into a 128-bit integer per output; the
+//     sum is exact.  One final conversion rounds it to FP64 (round to
+//     nearest even) and applies 2^(E_i + F_j).  No FP64 arithmetic is used
+//     until then: GB300's FP64 pipe delivers ~1 TFLOP/s, far below the
+//     integer and tensor paths.
+//
+// The integer tensor op (tcgen05 kind::i8) does not exist on sm_103a, and the
+// legacy warp-level IMMA path measured 151 TOP/s on GB300 against ~3.5
+// PFLOP/s for FP8, so the integer digits ride the FP8 pipe.
+//
+// GEMM kernel: persistent, warp-specialised; 128x256 output tile per CTA,
+// 128-byte-wide K blocks through a 4-stage TMA ring (48 KB/stage, 128-byte
+// swizzle), two 256-column FP32 accumulators in TMEM so that the epilogue of
+// one accumulator group overlaps the MMAs of the next.
+//   warp 0      TMA producer         warp 1   TMEM owner + MMA issuer
+//   warps 2..5  epilogue (TMEM -> registers -> 128-bit integer sums)
 #include "common.cuh"
 #include "runtime.hpp"
+#include "tc_common.cuh"
+#include "tma_host.hpp"
+
+#include <cuda_fp8.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <map>
+#include <mutex>
 
 namespace cgb {
-int ozaki_dgemm(const GemmDesc&, int, cudaStream_t, cosma_gpu_ozaki_info*) {
-    return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: not built yet");
+namespace oz {
+
+constexpr int BM = 128, BN = 256, BK = 128;  // BK in bytes = FP8 elements
+constexpr int STAGES = 4;
+constexpr int A_STAGE = BM * BK, B_STAGE = BN * BK, STAGE_BYTES = A_STAGE + B_STAGE;
+constexpr int THREADS = 192;
+constexpr int MAX_SLICES = 16;
+constexpr int MAX_UNITS = 144, MAX_GROUPS = 144;
+constexpr int64_t MAX_K_PER_CALL = 65536;  // 256 * k <= 2^24 for one product per accumulator
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+
+struct Schedule {
+    int n_groups;
+    int kb_count;           // K blocks of 128
+    int a_rows_pad, b_rows_pad;
+    uint8_t us[MAX_UNITS], ut[MAX_UNITS];        // slice indices (0-based) of each product
+    uint16_t gfirst[MAX_GROUPS];                 // first product of each accumulator group
+    uint8_t gcount[MAX_GROUPS], gshift[MAX_GROUPS];
+};
+
+struct GemmParams {
+    int num_m_tiles, num_tiles;
+    int64_t m, n, ldc;
+    double* C;
+    const int* expA;
+    const int* expB;
+    double alpha, beta;
+    int beta_zero, alpha_one;
+    int L;                 // value = V * 2^(E_i + F_j - L)
+    ulonglong2* W;         // per-CTA 128 x 256 128-bit partial sums
+    unsigned* err;
+    Schedule sched;
+};
+
+// --------------------------------------------------------------- scaling
+struct RowState {
+    int emax;     // floor(log2 max |x|) over the elements seen, INT_MIN/2 if none
+    float mass;   // sum of 2^(floor(log2|x|) - emax)
+};
+
+__device__ __forceinline__ float pow2f(int e) {  // 2^e as float, 0 below the normal range
+    return e < -126 ? 0.0f : __int_as_float((127 + e) << 23);
 }
+
+// floor(log2|x|) of a finite nonzero double from its bits; sets *bad for Inf/NaN.
+__device__ __forceinline__ bool element_log2(double x, int* lb, unsigned* bad) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    int ef = (int)((b >> 52) & 0x7FF);
+    unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+    if (ef == 0x7FF) { *bad = 1; return false; }
+    if (ef == 0) {
+        if (frac == 0) return false;
+        *lb = (63 - __clzll((long long)frac)) - 1074;
+        return true;
+    }
+    *lb = ef - 1023;
+    return true;
+}
+
+__device__ __forceinline__ void state_add(RowState& s, int lb) {
+    if (lb > s.emax) {
+        s.mass = s.mass * pow2f(s.emax - lb) + 1.0f;
+        s.emax = lb;
+    } else {
+        s.mass += pow2f(lb - s.emax);
+    }
+}
+__device__ __forceinline__ RowState state_merge(RowState a, RowState b) {
+    RowState r;
+    r.emax = max(a.emax, b.emax);
+    r.mass = a.mass * pow2f(a.emax - r.emax) + b.mass * pow2f(b.emax - r.emax);
+    return r;
+}
+
+struct Stats {
+    unsigned nonfinite;
+    float spread[2];  // max over rows of log2(2k / mass) for A rows / B columns
+};
+
+// Finishes one row: writes the scale exponent (E = emax + 1, 0 for zero
+// rows) and folds the row's spread estimate into the global maximum.
+__device__ __forceinline__ void finish_row(RowState s, int64_t k, int* exp_out, Stats* st, int which) {
+    if (s.mass <= 0.0f) {
+        *exp_out = 0;
+        return;
+    }
+    *exp_out = s.emax + 1;
+    float spread = log2f(2.0f * (float)k / s.mass);
+    if (spread < 0.0f) spread = 0.0f;
+    atomicMax((int*)&st->spread[which], __float_as_int(spread));  // non-negative floats order as ints
+}
+
+// Rows whose elements are contiguous along K (op(A) stored transposed, op(B)
+// stored as is): one warp per row.
+__global__ void scale_kcontig_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t k,
+                                     int* __restrict__ exp_out, Stats* st, int which) {
+    const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (row >= rows) return;
+    RowState s{-(1 << 30), 0.0f};
+    unsigned bad = 0;
+    const double* p = X + row * ld;
+    for (int64_t l = lane; l < k; l += 32) {
+        int lb;
+        if (element_log2(p[l], &lb, &bad)) state_add(s, lb);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        RowState t;
+        t.emax = __shfl_xor_sync(0xffffffffu, s.emax, o);
+        t.mass = __shfl_xor_sync(0xffffffffu, s.mass, o);
+        s = state_merge(s, t);
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&st->nonfinite, 1u);
+        finish_row(s, k, exp_out + row, st, which);
+    }
+}
+
+// Rows contiguous in memory (op(A) stored as is, op(B) stored transposed):
+// one thread per row over a chunk of K; partial states combined afterwards.
+__global__ void scale_mcontig_partial_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t k,
+                                             int64_t kchunk, int* __restrict__ pe, float* __restrict__ pm,
+                                             Stats* st) {
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows) return;
+    const int64_t l0 = (int64_t)blockIdx.y * kchunk, l1 = min(k, l0 + kchunk);
+    RowState s{-(1 << 30), 0.0f};
+    unsigned bad = 0;
+    for (int64_t l = l0; l < l1; ++l) {
+        int lb;
+        if (element_log2(X[row + l * ld], &lb, &bad)) state_add(s, lb);
+    }
+    if (bad) atomicOr(&st->nonfinite, 1u);
+    pe[blockIdx.y * rows + row] = s.emax;
+    pm[blockIdx.y * rows + row] = s.mass;
+}
+
+__global__ void scale_mcontig_combine_kernel(const int* __restrict__ pe, const float* __restrict__ pm, int nchunks,
+                                             int64_t rows, int64_t k, int* __restrict__ exp_out, Stats* st,
+                                             int which) {
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows) return;
+    RowState s{-(1 << 30), 0.0f};
+    for (int c = 0; c < nchunks; ++c) s = state_merge(s, RowState{pe[c * rows + row], pm[c * rows + row]});
+    finish_row(s, k, exp_out + row, st, which);
+}
+
+// --------------------------------------------------------------- slicing
+// Balanced base-32 digits of |x| / 2^E rounded to F = 4 + 5(S-1) fraction
+// bits (round half away from zero), most significant first, sign applied.
+template <int S>
+__device__ __forceinline__ void digits_of(double x, int E, int (&d)[S]) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const bool neg = (b >> 63) != 0;
+    const int ef = (int)((b >> 52) & 0x7FF);
+    unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+    int eu;
+    if (ef == 0) eu = -1074; else { M |= 1ull << 52; eu = ef - 1075; }
+    constexpr int F = 4 + 5 * (S - 1);
+    int sh = eu - E + F;  // X = M * 2^sh
+    if (M == 0) sh = 0;
+    if (sh < 0) {
+        const int r = -sh;
+        M = r > 63 ? 0ull : (M + (1ull << (r - 1))) >> r;
+        sh = 0;
+    }
+    int carry = 0;
+#pragma unroll
+    for (int p = 0; p < S; ++p) {
+        const int pos = 5 * p - sh;
+        unsigned long long v = pos >= 64 ? 0ull : (pos >= 0 ? (M >> pos) : (M << (-pos)));
+        int u = (p < S - 1) ? (int)(v & 31ull) : (int)v;
+        u += carry;
+        int dd = u;
+        if (p < S - 1) {
+            carry = u >= 16;
+            dd = carry ? u - 32 : u;
+        }
+        d[S - 1 - p] = neg ? -dd : dd;
+    }
+}
+
+__device__ __forceinline__ uint32_t pack4_e4m3(int a, int b, int c, int e) {
+    __nv_fp8x2_storage_t lo = __nv_cvt_float2_to_fp8x2(make_float2((float)a, (float)b), __NV_SATFINITE, __NV_E4M3);
+    __nv_fp8x2_storage_t hi = __nv_cvt_float2_to_fp8x2(make_float2((float)c, (float)e), __NV_SATFINITE, __NV_E4M3);
+    return (uint32_t)lo | ((uint32_t)hi << 16);
+}
+
+// Writes the S E4M3 digit slices of a (rows x k) operand, row-major with
+// row pitch k_pad, zero-padded to rows_pad x k_pad.  Each thread handles 16
+// consecutive K elements of one row.  kcontig: element (r, l) at X[l + r*ld],
+// else at X[r + l*ld].
+template <int S, bool KCONTIG>
+__global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows,
+                                                    int64_t k, const int* __restrict__ exps, int64_t k_pad,
+                                                    int64_t rows_pad, uint8_t* __restrict__ out) {
+    const int t = threadIdx.x;
+    int64_t r;
+    int kc;
+    if (KCONTIG) { r = (int64_t)blockIdx.x * 64 + t / 4; kc = t % 4; }
+    else { r = (int64_t)blockIdx.x * 64 + t % 64; kc = t / 64; }
+    const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 16;
+    if (r >= rows_pad || l0 >= k_pad) return;
+    const int E = r < rows ? exps[r] : 0;
+    uint32_t packed[S][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        int dg[4][S];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int64_t l = l0 + q * 4 + e;
+            double x = 0.0;
+            if (r < rows && l < k) x = KCONTIG ? X[l + r * ld] : X[r + l * ld];
+            digits_of<S>(x, E, dg[e]);
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s) packed[s][q] = pack4_e4m3(dg[0][s], dg[1][s], dg[2][s], dg[3][s]);
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        uint4 v = make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+        *reinterpret_cast<uint4*>(out + (int64_t)s * rows_pad * k_pad + r * k_pad + l0) = v;
+    }
+}
+
+// --------------------------------------------------- 128-bit recombination
+__device__ __forceinline__ void add_shifted(unsigned long long& lo, unsigned long long& hi, int x, int sh) {
+    const long long xs = x;
+    unsigned long long alo, ahi;
+    if (sh == 0) { alo = (unsigned long long)xs; ahi = (unsigned long long)(xs >> 63); }
+    else if (sh < 64) { alo = (unsigned long long)xs << sh; ahi = (unsigned long long)(xs >> (64 - sh)); }
+    else { alo = 0; ahi = (unsigned long long)(xs << (sh - 64)); }
+    const unsigned long long nlo = lo + alo;
+    hi = hi + ahi + (nlo < lo ? 1ull : 0ull);
+    lo = nlo;
+}
+
+// Round-to-nearest-even conversion of the signed 128-bit integer (hi:lo)
+// times 2^e2 to double (subnormal and overflow results included).
+__device__ __forceinline__ double i128_to_double(unsigned long long lo, unsigned long long hi, int e2) {
+    const bool neg = (long long)hi < 0;
+    if (neg) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0 ? 1ull : 0ull);
+    }
+    if (hi == 0 && lo == 0) return 0.0;
+    const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    int e_lsb = msb - 52 + e2;  // weight of the last kept bit for a normal result
+    int r = msb - 52;           // bits dropped
+    if (e_lsb < -1074) {        // subnormal result: fixed last-bit weight 2^-1074
+        r += -1074 - e_lsb;
+        e_lsb = -1074;
+    }
+    unsigned long long mant;
+    if (r <= 0) {
+        mant = lo << (-r);  // msb <= 52: the value fits in lo
+    } else if (r > 127) {
+        mant = 0;  // far below the smallest subnormal
+    } else {
+        // mant = V >> r, guard = bit r-1, sticky = bits below r-1
+        unsigned long long q, g, st;
+        if (r < 64) {
+            q = (lo >> r) | (hi << (64 - r));
+            g = (lo >> (r - 1)) & 1ull;
+            st = (r - 1) > 0 ? (lo & ((1ull << (r - 1)) - 1ull)) : 0ull;
+        } else if (r == 64) {
+            q = hi;
+            g = lo >> 63;
+            st = lo & 0x7FFFFFFFFFFFFFFFull;
+        } else {
+            q = hi >> (r - 64);
+            g = (hi >> (r - 65)) & 1ull;
+            st = lo | ((r - 65) > 0 ? (hi & ((1ull << (r - 65)) - 1ull)) : 0ull);
+        }
+        mant = q;
+        if (g && (st || (mant & 1ull))) ++mant;
+    }
+    unsigned long long bits;
+    const bool normal = e_lsb > -1074 || mant >= (1ull << 52);
+    if (mant >= (1ull << 53)) {  // rounding carried into a new bit
+        mant >>= 1;
+        ++e_lsb;
+    }
+    if (normal && mant >= (1ull << 52)) {
+        const int be = e_lsb + 52 + 1023;
+        if (be >= 2047) bits = 0x7FF0000000000000ull;
+        else bits = ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull);
+    } else {
+        bits = mant;  // subnormal (or the smallest normal reached by rounding)
+    }
+    if (neg) bits |= 0x8000000000000000ull;
+    return __longlong_as_double((long long)bits);
+}
+
+// ------------------------------------------------------------------ GEMM
+__global__ void __launch_bounds__(THREADS, 1)
+    ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                      const __grid_constant__ GemmParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf = empty + STAGES;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Schedule& sc = p.sched;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&accf[b], 1);
+            tc::mbar_init(&acce[b], 128);
+        }
+        tc::mbar_init(drain, 1);
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---------------------------------- TMA producer
+            uint32_t it = 0;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
+                const int mb = tile % p.num_m_tiles, nb = tile / p.num_m_tiles;
+                for (int g = 0; g < sc.n_groups && ok; ++g) {
+                    for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                        const int arow = sc.us[u] * sc.a_rows_pad + mb * BM;
+                        const int brow = sc.ut[u] * sc.b_rows_pad + nb * BN;
+                        for (int kb = 0; kb < sc.kb_count; ++kb, ++it) {
+                            const int st = it % STAGES;
+                            if (!tc::mbar_wait(&empty[st], ((it / STAGES) & 1) ^ 1, p.err, kDevTimeoutEmpty)) {
+                                ok = false;
+                                break;
+                            }
+                            tc::mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
+                            uint8_t* sa = smem + st * STAGE_BYTES;
+                            tc::tma_load_2d(sa, &tmA, kb * BK, arow, &full[st]);
+                            tc::tma_load_2d(sa + A_STAGE, &tmB, kb * BK, brow, &full[st]);
+                        }
+                    }
+                }
+            }
+            // let the copies in flight land before the CTA can exit
+            const uint32_t first = it > STAGES ? it - STAGES : 0;
+            for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, p.err, 0);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // ---------------------------------- MMA issuer
+            constexpr uint32_t ID = tc::idesc(tc::kFmtE4M3, tc::kFmtE4M3, BM, BN);
+            uint32_t it = 0, acc_it = 0;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
+                for (int g = 0; g < sc.n_groups && ok; ++g, ++acc_it) {
+                    const uint32_t buf = acc_it & 1;
+                    if (!tc::mbar_wait(&acce[buf], ((acc_it >> 1) & 1) ^ 1, p.err, kDevTimeoutAccEmpty)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t d_tmem = tmem + buf * BN;
+                    uint32_t accumulate = 0;
+                    for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                        for (int kb = 0; kb < sc.kb_count; ++kb, ++it) {
+                            const int st = it % STAGES;
+                            if (!tc::mbar_wait(&full[st], (it / STAGES) & 1, p.err, kDevTimeoutFull)) {
+                                ok = false;
+                                break;
+                            }
+                            tc::tc_fence_after();
+                            const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES);
+                            const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + A_STAGE);
+#pragma unroll
+                            for (int kk = 0; kk < BK / 32; ++kk) {
+                                tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
+                                accumulate = 1;
+                            }
+                            tc::mma_commit(&empty[st]);
+                        }
+                    }
+                    if (ok) tc::mma_commit(&accf[buf]);
+                }
+            }
+            // every MMA must be complete before TMEM is released
+            tc::mma_commit(drain);
+            tc::mbar_wait(drain, 0, p.err, 0);
+        }
+    } else {  // ------------------------------------------------ epilogue
+        const int quad = warp & 3;  // TMEM lanes this warp may access
+        const int row = quad * 32 + lane;
+        ulonglong2* W = p.W + (size_t)blockIdx.x * (BM * BN);
+        uint32_t acc_it = 0;
+        bool ok = true;
+        const int last = sc.n_groups - 1;
+        for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
+            const int mb = tile % p.num_m_tiles, nb = tile / p.num_m_tiles;
+            const int64_t gi = (int64_t)mb * BM + row;
+            const int Ei = p.expA[gi];
+            for (int g = 0; g <= last && ok; ++g, ++acc_it) {
+                const uint32_t buf = acc_it & 1;
+                // all lanes must agree before the warp-collective TMEM loads
+                ok = __all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, p.err, kDevTimeoutAcc));
+                if (!ok) break;
+                tc::tc_fence_after();
+                const int sh = sc.gshift[g];
+#pragma unroll 1
+                for (int c = 0; c < BN / 32; ++c) {
+                    uint32_t v[32];
+                    tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + buf * BN + c * 32, v);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int col = c * 32 + j;
+                        const int x = __float2int_rn(__uint_as_float(v[j]));
+                        ulonglong2* wp = W + col * BM + row;
+                        unsigned long long lo = 0, hi = 0;
+                        if (g > 0) {
+                            const ulonglong2 w = *wp;
+                            lo = w.x;
+                            hi = w.y;
+                        }
+                        add_shifted(lo, hi, x, sh);
+                        if (g < last) {
+                            *wp = make_ulonglong2(lo, hi);
+                        } else {
+                            const int64_t gj = (int64_t)nb * BN + col;
+                            if (gi < p.m && gj < p.n) {
+                                double r = i128_to_double(lo, hi, Ei + p.expB[gj] - p.L);
+                                double* cp = p.C + gi + gj * p.ldc;
+                                // C = fl(fl(alpha*r) + fl(beta*C)), no contraction
+                                if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
+                                if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+                                *cp = r;
+                            }
+                        }
+                    }
+                }
+                tc::tc_fence_before();
+                tc::mbar_arrive(&acce[buf]);
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, 512);
+    }
+}
+
+// ------------------------------------------------------------------ host
+struct Workspace {
+    DeviceBuffer slicesA, slicesB, expA, expB, part, W, stats, err;
+    Stats* host_stats = nullptr;
+    unsigned* host_err = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // prep start/end, gemm start/end
+};
+
+std::mutex g_ws_mu;
+std::map<std::pair<int, cudaStream_t>, Workspace*> g_ws;
+
+Workspace* workspace(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_ws_mu);
+    auto& w = g_ws[{dev, s}];
+    if (!w) {
+        w = new Workspace();
+        if (cudaMallocHost(&w->host_stats, sizeof(Stats)) != cudaSuccess) w->host_stats = nullptr;
+        if (cudaMallocHost(&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
+        for (auto& e : w->ev)
+            if (cudaEventCreate(&e) != cudaSuccess) e = nullptr;
+        cudaGetLastError();
+    }
+    return w;
+}
+
+int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = kNumSMs;
+    }
+    return n;
+}
+
+// Slice count from the requested accuracy and the measured exponent spread.
+// The fixed-point width F = 4 + 5(S-1) must reach ~1e-15 elementwise
+// relative error against an exactly rounded product.  Calibrated against the
+// double-double oracle on u*2^e inputs (u ~ U[-1,1], e ~ U{-phi..phi}): wider
+// exponent spreads need more bits (|A||B| falls short of k*sigma_i*sigma_j),
+// longer K needs fewer (the truncation errors average out against a C that
+// grows with k), and 60 bits are the floor for well-scaled data; 3 bits of
+// margin cover the worst-conditioned entries of larger samples.
+int choose_slices(double spread_bits, int64_t k) {
+    const double lk = std::log2((double)std::max<int64_t>(k, 1));
+    const double F = std::max(60.0, 65.0 + 0.75 * (spread_bits - 3.3) - (lk - 8.0));
+    int S = (int)std::ceil((F - 4.0) / 5.0) + 1;
+    return std::min(std::max(S, 2), MAX_SLICES);
+}
+
+int build_schedule(int S, int64_t k, int64_t k_pad, int a_rows_pad, int b_rows_pad, Schedule* sc, int* L) {
+    std::memset(sc, 0, sizeof(*sc));
+    sc->kb_count = (int)(k_pad / BK);
+    sc->a_rows_pad = a_rows_pad;
+    sc->b_rows_pad = b_rows_pad;
+    const int per_group = (int)std::max<int64_t>(1, MAX_K_PER_CALL / std::max<int64_t>(k, 1));
+    const int dmax = S + 1;  // 1-based diagonal index s + t of the last kept products
+    int nu = 0, ng = 0;
+    for (int d = 2; d <= dmax; ++d) {
+        const int s_lo = std::max(1, d - S), s_hi = std::min(S, d - 1);
+        for (int s0 = s_lo; s0 <= s_hi; s0 += per_group) {
+            if (ng >= MAX_GROUPS) return set_error(COSMA_GPU_ERROR_INTERNAL, "ozaki: schedule too long");
+            sc->gfirst[ng] = (uint16_t)nu;
+            int cnt = 0;
+            for (int s = s0; s <= std::min(s_hi, s0 + per_group - 1); ++s) {
+                if (nu >= MAX_UNITS) return set_error(COSMA_GPU_ERROR_INTERNAL, "ozaki: schedule too long");
+                sc->us[nu] = (uint8_t)(s - 1);
+                sc->ut[nu] = (uint8_t)(d - s - 1);
+                ++nu;
+                ++cnt;
+            }
+            sc->gcount[ng] = (uint8_t)cnt;
+            sc->gshift[ng] = (uint8_t)(5 * (dmax - d));
+            ++ng;
+        }
+    }
+    sc->n_groups = ng;
+    *L = 8 + 5 * (S - 1);
+    return COSMA_GPU_SUCCESS;
+}
+
+template <int S>
+void launch_split(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps, int64_t k_pad,
+                  int64_t rows_pad, uint8_t* out, cudaStream_t st) {
+    dim3 grid((unsigned)(rows_pad / 64), (unsigned)(k_pad / 64));
+    if (kcontig) split_kernel<S, true><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out);
+    else split_kernel<S, false><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out);
+}
+
+void split(int S, bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps, int64_t k_pad,
+           int64_t rows_pad, uint8_t* out, cudaStream_t st) {
+    switch (S) {
+#define CGB_SPLIT_CASE(n) case n: launch_split<n>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, st); break;
+        CGB_SPLIT_CASE(2) CGB_SPLIT_CASE(3) CGB_SPLIT_CASE(4) CGB_SPLIT_CASE(5) CGB_SPLIT_CASE(6) CGB_SPLIT_CASE(7)
+        CGB_SPLIT_CASE(8) CGB_SPLIT_CASE(9) CGB_SPLIT_CASE(10) CGB_SPLIT_CASE(11) CGB_SPLIT_CASE(12)
+        CGB_SPLIT_CASE(13) CGB_SPLIT_CASE(14) CGB_SPLIT_CASE(15) CGB_SPLIT_CASE(16)
+#undef CGB_SPLIT_CASE
+        default: break;
+    }
+}
+
+// Row scaling of a (rows x k) operand; kcontig as in split_kernel.
+int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, int* exps, Workspace* w,
+               Stats* st_dev, int which, cudaStream_t st) {
+    if (rows == 0) return COSMA_GPU_SUCCESS;
+    if (kcontig) {
+        scale_kcontig_kernel<<<(unsigned)ceil_div(rows, 8), 256, 0, st>>>(X, ld, rows, k, exps, st_dev, which);
+    } else {
+        const int64_t row_blocks = ceil_div(rows, 256);
+        int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
+        nchunks = (int)std::min<int64_t>(nchunks, std::max<int64_t>(1, k / 64));
+        const int64_t kchunk = ceil_div(k, nchunks);
+        CGB_CHECK(w->part.reserve((size_t)nchunks * rows * 8, st));
+        int* pe = (int*)w->part.ptr;
+        float* pm = (float*)((char*)w->part.ptr + (size_t)nchunks * rows * 4);
+        scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
+            X, ld, rows, k, kchunk, pe, pm, st_dev);
+        scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, rows, k, exps, st_dev,
+                                                                            which);
+    }
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
+}
+
+// One call with k <= MAX_K_PER_CALL.
+int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_info* info) {
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const bool ta = g.opa != 0, tb = g.opb != 0;
+    const double* A = (const double*)g.A;
+    const double* B = (const double*)g.B;
+    Workspace* w = workspace(st);
+    if (!w->host_stats || !w->host_err) return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "ozaki: pinned staging");
+    const int64_t m_pad = ceil_div(m, BM) * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BK) * BK;
+
+    // 1. scaling + spread statistics
+    CGB_CHECK(w->stats.reserve(sizeof(Stats), st));
+    CGB_CHECK(w->err.reserve(sizeof(unsigned), st));
+    CGB_CHECK(w->expA.reserve((size_t)m_pad * 4, st));
+    CGB_CHECK(w->expB.reserve((size_t)n_pad * 4, st));
+    Stats* st_dev = (Stats*)w->stats.ptr;
+    if (!w->ev[0] || !w->ev[3]) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki: timing events");
+    CGB_CUDA(cudaEventRecord(w->ev[0], st));
+    CGB_CUDA(cudaMemsetAsync(st_dev, 0, sizeof(Stats), st));
+    CGB_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(unsigned), st));
+    CGB_CUDA(cudaMemsetAsync(w->expA.ptr, 0, (size_t)m_pad * 4, st));
+    CGB_CUDA(cudaMemsetAsync(w->expB.ptr, 0, (size_t)n_pad * 4, st));
+    // op(A) row i: elements contiguous along K when A is stored transposed
+    CGB_CHECK(scale_rows(ta, A, g.lda, m, k, (int*)w->expA.ptr, w, st_dev, 0, st));
+    // op(B) column j: contiguous along K when B is stored as is
+    CGB_CHECK(scale_rows(!tb, B, g.ldb, n, k, (int*)w->expB.ptr, w, st_dev, 1, st));
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, st_dev, sizeof(Stats), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    const Stats hs = *w->host_stats;
+    const double spread = (double)hs.spread[0] + (double)hs.spread[1];
+    if (hs.nonfinite) {  // Inf/NaN cannot be sliced: the native FP64 kernel propagates them
+        if (info) info->fallback_native = 1;
+        return native_gemm(g, st);
+    }
+    const int S = slices > 0 ? std::min(slices, MAX_SLICES) : choose_slices(spread, k);
+    if (S < 2) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki: at least 2 slices");
+
+    // 2. slices
+    CGB_CHECK(w->slicesA.reserve((size_t)S * m_pad * k_pad, st));
+    CGB_CHECK(w->slicesB.reserve((size_t)S * n_pad * k_pad, st));
+    split(S, ta, A, g.lda, m, k, (const int*)w->expA.ptr, k_pad, m_pad, (uint8_t*)w->slicesA.ptr, st);
+    split(S, !tb, B, g.ldb, n, k, (const int*)w->expB.ptr, k_pad, n_pad, (uint8_t*)w->slicesB.ptr, st);
+    CGB_CUDA(cudaGetLastError());
+    CGB_CUDA(cudaEventRecord(w->ev[1], st));
+
+    // 3. slice products + recombination
+    GemmParams p;
+    std::memset(&p, 0, sizeof(p));
+    int L = 0;
+    CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &L));
+    p.num_m_tiles = (int)(m_pad / BM);
+    p.num_tiles = (int)((m_pad / BM) * (n_pad / BN));
+    p.m = m; p.n = n; p.ldc = g.ldc;
+    p.C = (double*)g.C;
+    p.expA = (const int*)w->expA.ptr;
+    p.expB = (const int*)w->expB.ptr;
+    p.alpha = g.alpha[0];
+    p.beta = g.beta[0];
+    p.beta_zero = g.beta[0] == 0.0;
+    p.alpha_one = g.alpha[0] == 1.0;
+    p.L = L;
+    const int grid = std::min(p.num_tiles, num_sms());
+    CGB_CHECK(w->W.reserve((size_t)grid * BM * BN * sizeof(ulonglong2), st));
+    p.W = (ulonglong2*)w->W.ptr;
+    p.err = (unsigned*)w->err.ptr;
+    CUtensorMap tmA, tmB;
+    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, w->slicesA.ptr, (uint64_t)k_pad,
+                           (uint64_t)(S * m_pad), (uint64_t)k_pad, BK, BM));
+    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, w->slicesB.ptr, (uint64_t)k_pad,
+                           (uint64_t)(S * n_pad), (uint64_t)k_pad, BK, BN));
+    static bool attr = false;
+    if (!attr) {
+        CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        attr = true;
+    }
+    CGB_CUDA(cudaEventRecord(w->ev[2], st));
+    ozaki_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
+    CGB_CUDA(cudaGetLastError());
+    CGB_CUDA(cudaEventRecord(w->ev[3], st));
+    CGB_CUDA(cudaMemcpyAsync(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    if (*w->host_err)
+        return set_error(COSMA_GPU_ERROR_DEVICE_TIMEOUT,
+                         "ozaki gemm: a pipeline wait timed out (device code " + std::to_string(*w->host_err) + ")");
+    if (info) {
+        int products = 0;
+        for (int i = 0; i < p.sched.n_groups; ++i) products += p.sched.gcount[i];
+        float prep = 0.f, gemm = 0.f;
+        cudaEventElapsedTime(&prep, w->ev[0], w->ev[1]);
+        cudaEventElapsedTime(&gemm, w->ev[2], w->ev[3]);
+        info->slices = S;
+        info->products = products;
+        info->groups = p.sched.n_groups;
+        info->spread_bits = spread;
+        info->prep_ms += prep;
+        info->gemm_ms += gemm;
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace oz
+
+int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
+    if (g.scalar != Scalar::D) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: double only");
+    if (((uintptr_t)g.A | (uintptr_t)g.B | (uintptr_t)g.C) % 8)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: buffers must be 8-byte aligned");
+    if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: m and n are limited to 2^24");
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    // K beyond one exact accumulator pass is cut into chunks accumulated
+    // through C (beta = 1 after the first chunk).
+    GemmDesc c = g;
+    for (int64_t k0 = 0; k0 < g.k; k0 += oz::MAX_K_PER_CALL) {
+        c.k = std::min<int64_t>(oz::MAX_K_PER_CALL, g.k - k0);
+        c.A = (const double*)g.A + (g.opa == 0 ? k0 * g.lda : k0);
+        c.B = (const double*)g.B + (g.opb == 0 ? k0 : k0 * g.ldb);
+        if (k0 > 0) { c.beta[0] = 1.0; c.beta[1] = 0.0; }
+        CGB_CHECK(oz::ozaki_chunk(c, slices, stream, info));
+        if (info && info->fallback_native) return COSMA_GPU_SUCCESS;
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
 }  // namespace cgb

@@ -62,6 +62,8 @@ typedef struct cosma_gpu_ozaki_info {
     int groups;          /* FP32 accumulator drains per output tile         */
     int fallback_native; /* 1 if non-finite input forced the native path    */
     double spread_bits;  /* exponent-spread estimate used to size slices    */
+    double prep_ms;      /* scaling + slicing kernels (CUDA events)         */
+    double gemm_ms;      /* slice-product GEMM kernel (CUDA events)         */
 } cosma_gpu_ozaki_info;
 
 /* ----------------------------------------------------- Tiled-MM interface */

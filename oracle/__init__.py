@@ -145,16 +145,40 @@ def pack(op, src, rows, cols, dst=None):
 def unpack(alpha, src, beta, dst):
     """dst = alpha*src + beta*dst (no read of dst when beta == 0), in place."""
     rows, cols = dst.shape
+    if src.dtype != dst.dtype:
+        raise TypeError("unpack: src and dst types differ")
     if dst.dtype == np.float64:
         lib().oracle_unpack_d(rows, cols, alpha, _p(src), _ld(src), beta, _p(dst), _ld(dst))
-    else:
+    elif dst.dtype == np.complex128:
         al = np.array([complex(alpha).real, complex(alpha).imag])
         be = np.array([complex(beta).real, complex(beta).imag])
         lib().oracle_unpack_z(rows, cols, _p(al), _p(src), _ld(src), _p(be), _p(dst), _ld(dst))
+    elif dst.dtype in (np.float32, np.complex64):
+        # single precision: numpy rounds every product and sum to the type
+        t = dst.dtype.type
+        ft = np.float32
+        if dst.dtype == np.float32:
+            v = t(alpha) * src[:rows, :cols]
+            if beta != 0:
+                v = v + t(beta) * dst[:rows, :cols]
+        else:
+            ar, ai = ft(complex(alpha).real), ft(complex(alpha).imag)
+            sr, si = src.real.astype(ft), src.imag.astype(ft)
+            vr, vi = ar * sr - ai * si, ar * si + ai * sr
+            if complex(beta) != 0:
+                br, bi = ft(complex(beta).real), ft(complex(beta).imag)
+                dr, di = dst.real.astype(ft), dst.imag.astype(ft)
+                vr, vi = vr + (br * dr - bi * di), vi + (br * di + bi * dr)
+            v = vr + 1j * vi
+        dst[:rows, :cols] = v
+    else:
+        raise TypeError(f"unpack: unsupported dtype {dst.dtype}")
     return dst
 
 
 def scale(beta, Cm):
+    if Cm.dtype != np.float64:
+        raise TypeError("scale: float64 only")
     lib().oracle_scale_d(Cm.shape[0], Cm.shape[1], beta, _p(Cm), _ld(Cm))
     return Cm
 

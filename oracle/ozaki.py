@@ -1,0 +1,99 @@
+"""CPU restatement of the Ozaki-split FP64 GEMM (test infrastructure only).
+
+The reference has no counterpart (it runs a native DGEMM); this restates the
+published error-free splitting (Ozaki, Ogita, Oishi & Rump 2012; integer
+slices as in Ootomo, Ozaki & Yokota 2024) exactly as the GPU kernels realise
+it, so their result can be checked bit for bit:
+  * E_i = 1 + floor(log2 max_l |a_il|) per row of op(A) (0 for zero rows),
+    F_j likewise per column of op(B);
+  * |a| / 2^E_i rounded half away from zero to F = 4 + 5(S-1) fraction bits,
+    written as balanced base-32 digits (leading digit 4 bits), sign applied;
+  * V_ij = sum over s + t <= S + 1 of (A_s B_t)_ij * 2^(5(S+1 - s - t)),
+    exact;
+  * C_ij = V_ij * 2^(E_i + F_j - 8 - 5(S-1)) rounded once to double.
+"""
+from __future__ import annotations
+
+from fractions import Fraction
+
+import numpy as np
+
+
+def row_exponents(X):
+    """E per row of X (rows x k): 1 + floor(log2 max |x|), 0 for zero rows."""
+    X = np.asarray(X, dtype=np.float64)
+    ax = np.abs(X)
+    mx = ax.max(axis=1) if X.shape[1] else np.zeros(X.shape[0])
+    E = np.zeros(X.shape[0], dtype=np.int64)
+    nz = mx > 0
+    E[nz] = np.frexp(mx[nz])[1]  # frexp: mx = f * 2^e with f in [0.5, 1) -> floor(log2) = e - 1
+    return E
+
+
+def digits(x, E, S):
+    """Digits (..., S) of x / 2^E, most significant first (vectorised)."""
+    x = np.asarray(x, dtype=np.float64)
+    E = np.asarray(E, dtype=np.int64)
+    b = x.view(np.uint64)
+    neg = (b >> np.uint64(63)) != 0
+    ef = ((b >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    M = b & np.uint64(0xFFFFFFFFFFFFF)
+    eu = np.where(ef == 0, -1074, ef - 1075)
+    M = np.where(ef == 0, M, M | np.uint64(1 << 52))
+    F = 4 + 5 * (S - 1)
+    sh = eu - E + F
+    sh = np.where(M == 0, 0, sh)
+    out = np.zeros(x.shape + (S,), dtype=np.int64)
+    neg_sh = sh < 0
+    r = np.where(neg_sh, -sh, 0)
+    # rounded X = (M + 2^(r-1)) >> r for sh < 0 (0 when r > 63)
+    Mr = M.copy()
+    rr = np.clip(r, 1, 63).astype(np.uint64)
+    rounded = (M + (np.uint64(1) << (rr - np.uint64(1)))) >> rr
+    Mr = np.where(neg_sh, np.where(r > 63, np.uint64(0), rounded), M)
+    sh = np.where(neg_sh, 0, sh)
+    carry = np.zeros(x.shape, dtype=np.int64)
+    for p in range(S):
+        pos = 5 * p - sh
+        right = np.clip(pos, 0, 63).astype(np.uint64)
+        left = np.clip(-pos, 0, 63).astype(np.uint64)
+        v = np.where(pos >= 64, np.uint64(0), np.where(pos >= 0, Mr >> right, Mr << left))
+        u = (v & np.uint64(31)).astype(np.int64) if p < S - 1 else v.astype(np.int64)
+        u = u + carry
+        if p < S - 1:
+            carry = (u >= 16).astype(np.int64)
+            dd = np.where(carry == 1, u - 32, u)
+        else:
+            dd = u
+        out[..., S - 1 - p] = np.where(neg, -dd, dd)
+    return out
+
+
+def ozaki_gemm(ta, tb, A, B, S):
+    """Exact restatement of the GPU result for alpha = 1, beta = 0 (small sizes)."""
+    opA = np.asarray(A if ta in "Nn" else A.T, dtype=np.float64)
+    opB = np.asarray(B if tb in "Nn" else B.T, dtype=np.float64)
+    m, k = opA.shape
+    n = opB.shape[1]
+    EA = row_exponents(opA)
+    EB = row_exponents(opB.T)
+    DA = digits(opA, EA[:, None], S)          # m x k x S
+    DB = digits(opB.T, EB[:, None], S)        # n x k x S
+    L = 8 + 5 * (S - 1)
+    V = np.zeros((m, n), dtype=object)
+    for s in range(1, S + 1):
+        for t in range(1, S + 2 - s):
+            P = DA[:, :, s - 1] @ DB[:, :, t - 1].T  # exact in int64 for k <= 2^46
+            V = V + P.astype(object) * (1 << (5 * (S + 1 - s - t)))
+    C = np.zeros((m, n))
+    for i in range(m):
+        for j in range(n):
+            e = int(EA[i] + EB[j] - L)
+            v = Fraction(int(V[i, j])) * (Fraction(2) ** e)
+            C[i, j] = float(v)
+    return C
+
+
+def error_bound_bits(S):
+    """Fraction bits F = 4 + 5(S-1) carried by S slices."""
+    return 4 + 5 * (S - 1)

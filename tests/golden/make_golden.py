@@ -92,18 +92,18 @@ def block_cyclic_cases():
 
 
 def balanced_digits(x: float, e_row: int, nslices: int):
-    """Balanced digits d_1..d_S of x / 2**e_row in base 32 with a 4-bit first
-    digit: x / 2**e_row ~= sum_s d_s * 2**(-4 - 5*(s-1)), |d_s| <= 16, the
-    value rounded to nearest (ties away from zero) at 2**-(4+5(S-1))."""
+    """Digits d_1..d_S of x / 2**e_row with a 4-bit first digit and 5-bit
+    digits after it: |x| / 2**e_row is rounded to F = 4 + 5(S-1) fraction
+    bits (half away from zero), written in balanced base 32 (every digit in
+    [-16, 15] except the leading one, in [0, 16]), and the sign of x applied
+    to every digit, so x / 2**e_row ~= sum_s d_s 2**(-4 - 5(s-1))."""
     F = 4 + 5 * (nslices - 1)
     v = Fraction(x) / Fraction(2) ** e_row * Fraction(2) ** F
-    # round half away from zero
     sgn = -1 if v < 0 else 1
     a = abs(v)
     X = int(a)
     if a - X >= Fraction(1, 2):
         X += 1
-    X *= sgn
     digits = []
     for _ in range(nslices - 1):
         d = ((X + 16) % 32) - 16
@@ -111,6 +111,7 @@ def balanced_digits(x: float, e_row: int, nslices: int):
         X = (X - d) // 32
     digits.append(X)
     digits.reverse()
+    digits = [sgn * d for d in digits]
     assert all(abs(d) <= 16 for d in digits), digits
     return digits
 

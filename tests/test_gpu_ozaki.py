@@ -1,0 +1,144 @@
+"""Ozaki-split FP64-accurate GEMM on the FP8 tensor cores vs the oracle.
+
+* bit-exact against the CPU restatement of the same algorithm (oracle/ozaki.py)
+  on small sizes, every op combination;
+* exactness of the FP32 accumulation: integer inputs give the exact integer
+  product at K = 16384 (sums up to 2^24 inside one accumulator);
+* accuracy against the double-double oracle (max elementwise relative error
+  <= 1e-15, and <= 2^-52 |A||B| componentwise) for the precision
+  configuration's distributions, phi in {0, 8, 32};
+* edge cases: ragged sizes, k = 1, k above one exact accumulator pass, alpha
+  and beta, beta == 0 with NaN in C, non-finite inputs.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import from_dev, to_dev
+from oracle import ozaki as oz
+
+pytestmark = pytest.mark.gpu
+
+
+def _op_shape(op, m, k):
+    return (m, k) if op == "N" else (k, m)
+
+
+def _run(ta, tb, m, n, k, A, B, alpha=1.0, beta=0.0, C0=None, slices=0, lda=None, ldb=None, ldc=None):
+    from cosma_gb300 import dgemm_ozaki_device
+    lda = lda or A.shape[0]
+    ldb = ldb or B.shape[0]
+    ldc = ldc or m
+    dA, dB = to_dev(A, lda), to_dev(B, ldb)
+    dC = to_dev(C0 if C0 is not None else np.zeros((m, n)), ldc)
+    info = dgemm_ozaki_device(ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, slices=slices)
+    return from_dev(dC, m, n, ldc), info
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+@pytest.mark.parametrize("m,n,k,S", [(17, 9, 33, 4), (64, 40, 130, 7), (130, 260, 200, 13), (5, 300, 129, 16)])
+def test_bit_exact_against_restatement(native_lib, cuda, ta, tb, m, n, k, S):
+    A = oracle.exp_spread(_op_shape(ta, m, k), m + k, 6)
+    B = oracle.exp_spread(_op_shape(tb, k, n), n + k, 6)
+    got, info = _run(ta, tb, m, n, k, A, B, slices=S, lda=A.shape[0] + 1, ldc=m + 3)
+    ref = oz.ozaki_gemm(ta, tb, A, B, S)
+    assert info["slices"] == S and info["products"] == S * (S + 1) // 2
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_fp32_accumulation_is_exact_at_k16384(native_lib, cuda):
+    rng = np.random.default_rng(1)
+    m, n, k = 256, 256, 16384
+    A = np.asfortranarray(rng.integers(-15, 16, (m, k)).astype(np.float64))
+    B = np.asfortranarray(rng.integers(-15, 16, (k, n)).astype(np.float64))
+    # all-maximal digits in a few rows/cols stress the 2^24 bound
+    A[:4, :] = 15.0
+    B[:, :4] = 15.0
+    got, info = _run("N", "N", m, n, k, A, B, slices=4)
+    exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    assert info["groups"] < info["products"]  # several products share one accumulator
+    np.testing.assert_array_equal(got, exact)
+
+
+@pytest.mark.parametrize("phi", [0, 8, 32])
+def test_accuracy_against_double_double(native_lib, cuda, phi):
+    m = n = 384
+    k = 2048
+    A = oracle.exp_spread((m, k), 10 + phi, phi)
+    B = oracle.exp_spread((k, n), 20 + phi, phi)
+    got, info = _run("N", "N", m, n, k, A, B)
+    rng = np.random.default_rng(phi)
+    rows = rng.integers(0, m, 2048)
+    cols = rng.integers(0, n, 2048)
+    hi, lo, ab = oracle.gemm_dd_sampled("N", "N", A, B, rows, cols)
+    st = oracle.error_stats(got[rows, cols], hi, lo, ab)
+    assert st["max_rel_err"] <= 1e-15, (st, info)
+    assert st["max_err_over_absab"] <= 2.0 ** -52, (st, info)
+
+
+def test_alpha_beta_and_nan_c(native_lib, cuda):
+    m, n, k = 100, 70, 90
+    A, B = oracle.uniform((m, k), 1), oracle.uniform((k, n), 2)
+    C0 = oracle.uniform((m, n), 3)
+    S = 12
+    base = oz.ozaki_gemm("N", "N", A, B, S)
+    got, _ = _run("N", "N", m, n, k, A, B, alpha=1.5, beta=-0.5, C0=C0, slices=S)
+    np.testing.assert_array_equal(got, 1.5 * base + (-0.5) * C0)
+    nanc = np.full((m, n), np.nan)
+    got, _ = _run("N", "N", m, n, k, A, B, alpha=2.0, beta=0.0, C0=nanc, slices=S)
+    np.testing.assert_array_equal(got, 2.0 * base)
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (1, 257, 3), (129, 1, 257), (7, 300, 1)])
+def test_ragged_sizes(native_lib, cuda, m, n, k):
+    A, B = oracle.uniform((m, k), m), oracle.uniform((k, n), n)
+    got, _ = _run("N", "N", m, n, k, A, B, slices=13)
+    np.testing.assert_array_equal(got, oz.ozaki_gemm("N", "N", A, B, 13))
+
+
+def test_k_beyond_one_accumulator_pass(native_lib, cuda):
+    # k > 65536 is processed in exact passes accumulated through C
+    m, n, k = 8, 8, 70000
+    A, B = oracle.uniform((m, k), 5), oracle.uniform((k, n), 6)
+    got, info = _run("N", "N", m, n, k, A, B)
+    hi, lo, ab = oracle.gemm_dd("N", "N", A, B)
+    st = oracle.error_stats(got, hi, lo, ab)
+    assert st["max_err_over_absab"] <= 2.0 ** -51
+
+
+def test_nonfinite_inputs_fall_back_to_native(native_lib, cuda):
+    m, n, k = 40, 30, 20
+    A, B = oracle.uniform((m, k), 7), oracle.uniform((k, n), 8)
+    A[3, 4] = np.inf
+    A[5, 6] = np.nan
+    got, info = _run("N", "N", m, n, k, A, B)
+    assert info["fallback_native"] == 1
+    ref = A @ B
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(ref))
+
+
+def test_auto_slices_follow_spread(native_lib, cuda):
+    m = n = 256
+    k = 1024
+    s = {}
+    for phi in (0, 32):
+        A = oracle.exp_spread((m, k), 1, phi)
+        B = oracle.exp_spread((k, n), 2, phi)
+        _, info = _run("N", "N", m, n, k, A, B)
+        s[phi] = info["slices"]
+    assert s[32] > s[0]
+
+
+def test_tiled_mm_handle_with_ozaki_method(native_lib, cuda):
+    from cosma_gb300 import gemm, make_context
+    h = make_context("d", 2, 200, 200, 300)
+    h.set_method("ozaki", 13)
+    m, n, k = 333, 222, 700
+    A, B = oracle.uniform((m, k), 11), oracle.uniform((n, k), 12)
+    Cg = np.zeros((m, n), order="F")
+    gemm(h, "N", "T", m, n, k, 1.0, A, m, B, n, 0.0, Cg, m)
+    hi, lo, ab = oracle.gemm_dd("N", "T", A, B)
+    st = oracle.error_stats(Cg, hi, lo, ab)
+    assert st["max_err_over_absab"] <= 2.0 ** -51  # K tiles add one rounding each
+    assert h.ozaki_info()["slices"] == 13
+    h.close()

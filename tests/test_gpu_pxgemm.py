@@ -12,6 +12,8 @@ pytestmark = pytest.mark.gpu
 def _run_case(ma, na, mb_, nb_, mc, nc, bma, bna, bmb, bnb, bmc, bnc, ia, ja, ib, jb, ic, jc, m, n, k, ta, tb,
               alpha, beta, lld_a, lld_b, lld_c, seed=0, dtype=np.float64, prefix="p", suffix="_", method=None):
     from cosma_gb300 import descinit, pxgemm, pxgemm_set_method
+    ta_lib, tb_lib = ta, tb          # flags as the caller passes them (any case)
+    ta, tb = ta.upper(), tb.upper()  # the reference upper-cases them (cosma_pxgemm.cpp:57-58)
     rng_seed = seed * 7919 + m * 31 + n * 17 + k
     A = oracle.uniform((lld_a, na), rng_seed + 1, 0.0, 1.0, dtype=dtype)  # random_generator: U[0, 1)
     B = oracle.uniform((lld_b, nb_), rng_seed + 2, 0.0, 1.0, dtype=dtype)
@@ -37,8 +39,8 @@ def _run_case(ma, na, mb_, nb_, mc, nc, bma, bna, bmb, bnb, bmc, bnc, ia, ja, ib
     if method:
         pxgemm_set_method(method)
     try:
-        pxgemm(ta, tb, m, n, k, alpha, A, ia, ja, desca, B, ib, jb, descb, beta, C, ic, jc, descc, prefix=prefix,
-               suffix=suffix)
+        pxgemm(ta_lib, tb_lib, m, n, k, alpha, A, ia, ja, desca, B, ib, jb, descb, beta, C, ic, jc, descc,
+               prefix=prefix, suffix=suffix)
     finally:
         if method:
             pxgemm_set_method("native")
