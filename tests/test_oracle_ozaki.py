@@ -61,7 +61,7 @@ def test_accuracy_against_double_double(phi):
     A = oracle.exp_spread((24, 300), 11 + phi, phi)
     B = oracle.exp_spread((300, 20), 12 + phi, phi)
     hi, lo, ab = oracle.gemm_dd("N", "N", A, B)
-    S = 13
+    S = 16  # short K with a wide exponent spread needs the full slice budget
     C = ozaki.ozaki_gemm("N", "N", A, B, S)
     st = oracle.error_stats(C, hi, lo, ab)
     assert st["max_err_over_absab"] < 2.0 ** -52
