@@ -74,7 +74,7 @@ struct Schedule {
 };
 
 struct GemmParams {
-    int num_m_tiles, num_tiles;
+    int num_m_tiles, num_n_tiles, num_tiles;
     int64_t m, n, ldc;
     double* C;
     const int* expA;
@@ -350,6 +350,19 @@ __device__ __forceinline__ double i128_to_double(unsigned long long lo, unsigned
 }
 
 // ------------------------------------------------------------------ GEMM
+// Tile order: strips of kStripM M-tiles, N-tiles within a strip, M-tiles
+// fastest.  The 152 CTAs of one wave then cover a ~16 x 10 block of tiles,
+// so every A- and B-slice panel a wave needs is fetched from HBM once and
+// served to the other CTAs of its row / column from L2.
+constexpr int kStripM = 16;
+__device__ __forceinline__ void tile_coords(int tile, int num_m, int num_n, int& mb, int& nb) {
+    const int strip = tile / (kStripM * num_n);
+    const int r = tile - strip * kStripM * num_n;
+    const int h = min(kStripM, num_m - strip * kStripM);  // the last strip may be shorter
+    nb = r / h;
+    mb = strip * kStripM + r % h;
+}
+
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ GemmParams p) {
@@ -389,7 +402,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t it = 0;
             bool ok = true;
             for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
-                const int mb = tile % p.num_m_tiles, nb = tile / p.num_m_tiles;
+                int mb, nb;
+                tile_coords(tile, p.num_m_tiles, p.num_n_tiles, mb, nb);
                 for (int g = 0; g < sc.n_groups && ok; ++g) {
                     for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
                         const int arow = sc.us[u] * sc.a_rows_pad + mb * BM;
@@ -460,7 +474,8 @@ __global__ void __launch_bounds__(THREADS, 1)
         bool ok = true;
         const int last = sc.n_groups - 1;
         for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
-            const int mb = tile % p.num_m_tiles, nb = tile / p.num_m_tiles;
+            int mb, nb;
+            tile_coords(tile, p.num_m_tiles, p.num_n_tiles, mb, nb);
             const int64_t gi = (int64_t)mb * BM + row;
             const int Ei = p.expA[gi];
             for (int g = 0; g <= last && ok; ++g, ++acc_it) {
@@ -562,7 +577,7 @@ int num_sms() {
 // margin cover the worst-conditioned entries of larger samples.
 int choose_slices(double spread_bits, int64_t k) {
     const double lk = std::log2((double)std::max<int64_t>(k, 1));
-    const double F = std::max(60.0, 65.0 + 0.75 * (spread_bits - 3.3) - (lk - 8.0));
+    const double F = std::max(60.0, 65.0 + 0.85 * (spread_bits - 3.3) - (lk - 8.0));
     int S = (int)std::ceil((F - 4.0) / 5.0) + 1;
     return std::min(std::max(S, 2), MAX_SLICES);
 }
@@ -692,6 +707,7 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
     int L = 0;
     CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &L));
     p.num_m_tiles = (int)(m_pad / BM);
+    p.num_n_tiles = (int)(n_pad / BN);
     p.num_tiles = (int)((m_pad / BM) * (n_pad / BN));
     p.m = m; p.n = n; p.ldc = g.ldc;
     p.C = (double*)g.C;
