@@ -774,8 +774,8 @@ int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
         c.A = (const double*)g.A + (g.opa == 0 ? k0 * g.lda : k0);
         c.B = (const double*)g.B + (g.opb == 0 ? k0 : k0 * g.ldb);
         if (k0 > 0) { c.beta[0] = 1.0; c.beta[1] = 0.0; }
+        // a chunk holding Inf/NaN runs on the native kernel; the others stay split
         CGB_CHECK(oz::ozaki_chunk(c, slices, stream, info));
-        if (info && info->fallback_native) return COSMA_GPU_SUCCESS;
     }
     return COSMA_GPU_SUCCESS;
 }
