@@ -57,6 +57,8 @@ SIGNATURES = {
     "cosma_gpu_cgemm_device": (i32, [i32, ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "cosma_gpu_dgemm_ozaki_device": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                            C.POINTER(OzakiInfo)]),
+    "cosma_gpu_dgemm_ozaki_noalloc": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
+                                            C.POINTER(OzakiInfo)]),
     "costa_gpu_pack": (i32, [ch, i32, i32, i64, i64, vp, i64, vp, i64, vp]),
     "costa_gpu_unpack_d": (i32, [i64, i64, dbl, vp, i64, dbl, vp, i64, vp]),
     "costa_gpu_unpack_s": (i32, [i64, i64, flt, vp, i64, flt, vp, i64, vp]),

@@ -780,4 +780,242 @@ int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
     return COSMA_GPU_SUCCESS;
 }
 
+// ===========================================================================
+// Ozaki DGEMM without any allocation.
+//
+// Who needs it: callers that cannot let a library call cudaMalloc or cudaFree.
+// A solver or framework plugin that has handed all device memory to its own
+// pool allocator has nothing left for a library to allocate, and code that
+// keeps copies and kernels overlapping on several streams cannot afford the
+// device-wide synchronisation that cudaMalloc and cudaFree imply.  For them
+// the same kernels run with every scratch buffer (exponents, statistics,
+// digit slices, partial sums) carved out of one statically sized device
+// array, g_noalloc_scratch, which the module keeps on every GPU that loads
+// the library until the process exits.
+// ===========================================================================
+namespace oz {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)COSMA_GPU_OZAKI_NOALLOC_SCRATCH_BYTES;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device with that device current.  In host code the array's name only
+// stands for a host-side shadow; a kernel handed it would fault or touch the
+// wrong memory, so kernels only ever get the address returned here.
+int noalloc_scratch_address(void** out) {
+    int dev = 0;
+    CGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki no-alloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(no-alloc scratch)");
+        if (!p) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki no-alloc: null scratch address");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return COSMA_GPU_SUCCESS;
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// K chunks of the row-exponent pass for rows contiguous in memory (the same
+// split scale_rows uses, so both entry points pick the same slice count).
+inline int mcontig_chunks(int64_t rows, int64_t k) {
+    const int64_t row_blocks = ceil_div(rows, 256);
+    int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
+    return (int)std::min<int64_t>(nchunks, std::max<int64_t>(1, k / 64));
+}
+
+// Byte offsets of the scratch buffers inside g_noalloc_scratch.
+struct NoAllocLayout {
+    size_t stats, err, expA, expB, part, head;  // slice-count independent part
+    size_t slicesA, slicesB, W, total;
+};
+
+NoAllocLayout noalloc_layout(int64_t m, int64_t n, int64_t k, int S, bool a_kcontig, bool b_kcontig) {
+    const int64_t m_pad = ceil_div(m, BM) * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BK) * BK;
+    NoAllocLayout L;
+    size_t off = 0;
+    L.stats = off; off += align256(sizeof(Stats));
+    L.err = off; off += align256(sizeof(unsigned));
+    L.expA = off; off += align256((size_t)m_pad * 4);
+    L.expB = off; off += align256((size_t)n_pad * 4);
+    size_t part = 0;
+    if (!a_kcontig) part = std::max(part, (size_t)mcontig_chunks(m, k) * m * 8);
+    if (!b_kcontig) part = std::max(part, (size_t)mcontig_chunks(n, k) * n * 8);
+    L.part = off; off += align256(part);
+    L.head = off;
+    L.slicesA = off; off += align256((size_t)S * m_pad * k_pad);
+    L.slicesB = off; off += align256((size_t)S * n_pad * k_pad);
+    const int64_t tiles = (m_pad / BM) * (n_pad / BN);
+    L.W = off; off += align256((size_t)std::min<int64_t>(tiles, num_sms()) * BM * BN * sizeof(ulonglong2));
+    L.total = off;
+    return L;
+}
+
+int too_large(size_t need) {
+    return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT,
+                     "ozaki no-alloc: the problem needs " + std::to_string(need) + " bytes of scratch, more than the " +
+                         std::to_string(kNoAllocScratchBytes) +
+                         "-byte static array (use cosma_gpu_dgemm_ozaki_device for larger problems)");
+}
+
+// One pass over K (k <= MAX_K_PER_CALL), the no-alloc twin of ozaki_chunk.
+int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_info* info) {
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const bool ta = g.opa != 0, tb = g.opb != 0;
+    const double* A = (const double*)g.A;
+    const double* B = (const double*)g.B;
+    const int64_t m_pad = ceil_div(m, BM) * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BK) * BK;
+    // Reject before touching the device: the smallest slice count must fit.
+    const NoAllocLayout L2 = noalloc_layout(m, n, k, slices > 0 ? std::min(slices, MAX_SLICES) : 2, ta, !tb);
+    if (L2.total > kNoAllocScratchBytes) return too_large(L2.total);
+    void* base = nullptr;
+    CGB_CHECK(noalloc_scratch_address(&base));
+    char* sc = (char*)base;
+    Stats* st_dev = (Stats*)(sc + L2.stats);
+    unsigned* err_dev = (unsigned*)(sc + L2.err);
+    int* expA = (int*)(sc + L2.expA);
+    int* expB = (int*)(sc + L2.expB);
+    char* part = sc + L2.part;
+
+    // 1. scaling + spread statistics; the array keeps the previous call's
+    //    contents, so everything read before being written is cleared first.
+    CGB_CUDA(cudaMemsetAsync(st_dev, 0, sizeof(Stats), st));
+    CGB_CUDA(cudaMemsetAsync(err_dev, 0, sizeof(unsigned), st));
+    CGB_CUDA(cudaMemsetAsync(expA, 0, (size_t)m_pad * 4, st));
+    CGB_CUDA(cudaMemsetAsync(expB, 0, (size_t)n_pad * 4, st));
+    struct Operand { bool kcontig; const double* X; int64_t ld, rows; int* exps; int which; };
+    const Operand ops[2] = {{ta, A, g.lda, m, expA, 0}, {!tb, B, g.ldb, n, expB, 1}};
+    for (const Operand& o : ops) {
+        if (o.rows == 0) continue;
+        if (o.kcontig) {
+            scale_kcontig_kernel<<<(unsigned)ceil_div(o.rows, 8), 256, 0, st>>>(o.X, o.ld, o.rows, k, o.exps, st_dev,
+                                                                                 o.which);
+        } else {
+            const int64_t row_blocks = ceil_div(o.rows, 256);
+            const int nchunks = mcontig_chunks(o.rows, k);
+            const int64_t kchunk = ceil_div(k, nchunks);
+            int* pe = (int*)part;
+            float* pm = (float*)(part + (size_t)nchunks * o.rows * 4);
+            scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
+                o.X, o.ld, o.rows, k, kchunk, pe, pm, st_dev);
+            scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, o.rows, k, o.exps,
+                                                                                st_dev, o.which);
+        }
+        CGB_CUDA(cudaGetLastError());
+    }
+    Stats hs;
+    CGB_CUDA(cudaMemcpyAsync(&hs, st_dev, sizeof(Stats), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    const double spread = (double)hs.spread[0] + (double)hs.spread[1];
+    if (hs.nonfinite) {
+        if (info) info->fallback_native = 1;
+        return native_gemm(g, st);  // the native kernel needs no scratch
+    }
+    const int S = slices > 0 ? std::min(slices, MAX_SLICES) : choose_slices(spread, k);
+    if (S < 2) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki: at least 2 slices");
+    const NoAllocLayout L = noalloc_layout(m, n, k, S, ta, !tb);
+    if (L.total > kNoAllocScratchBytes) return too_large(L.total);
+
+    // 2. slices (every byte, padding included, is rewritten)
+    uint8_t* slA = (uint8_t*)(sc + L.slicesA);
+    uint8_t* slB = (uint8_t*)(sc + L.slicesB);
+    split(S, ta, A, g.lda, m, k, expA, k_pad, m_pad, slA, st);
+    split(S, !tb, B, g.ldb, n, k, expB, k_pad, n_pad, slB, st);
+    CGB_CUDA(cudaGetLastError());
+
+    // 3. slice products + recombination (the partial sums are written before
+    //    they are read in every tile, so they need no clearing)
+    GemmParams p;
+    std::memset(&p, 0, sizeof(p));
+    int Lw = 0;
+    CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &Lw));
+    p.num_m_tiles = (int)(m_pad / BM);
+    p.num_n_tiles = (int)(n_pad / BN);
+    p.num_tiles = (int)((m_pad / BM) * (n_pad / BN));
+    p.m = m; p.n = n; p.ldc = g.ldc;
+    p.C = (double*)g.C;
+    p.expA = expA;
+    p.expB = expB;
+    p.alpha = g.alpha[0];
+    p.beta = g.beta[0];
+    p.beta_zero = g.beta[0] == 0.0;
+    p.alpha_one = g.alpha[0] == 1.0;
+    p.L = Lw;
+    p.W = (ulonglong2*)(sc + L.W);
+    p.err = err_dev;
+    const int grid = std::min(p.num_tiles, num_sms());
+    CUtensorMap tmA, tmB;
+    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slA, (uint64_t)k_pad, (uint64_t)(S * m_pad),
+                           (uint64_t)k_pad, BK, BM));
+    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slB, (uint64_t)k_pad, (uint64_t)(S * n_pad),
+                           (uint64_t)k_pad, BK, BN));
+    CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    ozaki_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
+    CGB_CUDA(cudaGetLastError());
+    unsigned herr = 0;
+    CGB_CUDA(cudaMemcpyAsync(&herr, err_dev, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    if (herr)
+        return set_error(COSMA_GPU_ERROR_DEVICE_TIMEOUT,
+                         "ozaki gemm: a pipeline wait timed out (device code " + std::to_string(herr) + ")");
+    if (info) {
+        int products = 0;
+        for (int i = 0; i < p.sched.n_groups; ++i) products += p.sched.gcount[i];
+        info->slices = S;
+        info->products = products;
+        info->groups = p.sched.n_groups;
+        info->spread_bits = spread;
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace oz
 }  // namespace cgb
+
+extern "C" int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k, double alpha,
+                                             const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                                             double* C, int64_t ldc, int slices, void* stream,
+                                             cosma_gpu_ozaki_info* info) {
+    using namespace cgb;
+    clear_error();
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    const int opa = parse_op(transa), opb = parse_op(transb);
+    if (opa < 0 || opb < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: op must be N, T or C");
+    if (m < 0 || n < 0 || k < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: negative size");
+    if (m == 0 || n == 0) return COSMA_GPU_SUCCESS;
+    const int64_t a_rows = opa == 0 ? m : k, b_rows = opb == 0 ? k : n;
+    if (ldc < std::max<int64_t>(1, m) ||
+        (k > 0 && (lda < std::max<int64_t>(1, a_rows) || ldb < std::max<int64_t>(1, b_rows))))
+        return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: leading dimension too small");
+    if (((uintptr_t)A | (uintptr_t)B | (uintptr_t)C) % 8)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki no-alloc: buffers must be 8-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    double be[2] = {beta, 0.0};
+    if (k == 0 || alpha == 0.0) return scale_matrix_device(Scalar::D, m, n, be, C, ldc, st);
+    GemmDesc g;
+    g.scalar = Scalar::D;
+    g.opa = opa;
+    g.opb = opb;
+    g.m = m; g.n = n; g.k = k;
+    g.alpha[0] = alpha; g.alpha[1] = 0.0;
+    g.beta[0] = beta; g.beta[1] = 0.0;
+    g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.C = C; g.ldc = ldc;
+    GemmDesc c = g;
+    for (int64_t k0 = 0; k0 < k; k0 += oz::MAX_K_PER_CALL) {
+        c.k = std::min<int64_t>(oz::MAX_K_PER_CALL, k - k0);
+        c.A = A + (opa == 0 ? k0 * lda : k0);
+        c.B = B + (opb == 0 ? k0 : k0 * ldb);
+        if (k0 > 0) c.beta[0] = 1.0;
+        CGB_CHECK(oz::noalloc_chunk(c, slices, st, info));
+    }
+    return COSMA_GPU_SUCCESS;
+}

@@ -154,6 +154,29 @@ int cosma_gpu_dgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n,
                                  int64_t ldb, double beta, double* C, int64_t ldc, int slices,
                                  void* stream, cosma_gpu_ozaki_info* info);
 
+/* Size of the static device array that cosma_gpu_dgemm_ozaki_noalloc draws
+ * all of its scratch from (64 MiB, held on every GPU that loads the library). */
+#define COSMA_GPU_OZAKI_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* FP64-accurate Ozaki-split DGEMM that allocates nothing; it has no
+ * counterpart in the reference.  It is meant for callers that cannot let a
+ * library allocate device memory: applications whose device memory is all
+ * owned by their own pool allocator, and code that must not trigger the
+ * device-wide synchronisation cudaMalloc / cudaFree imply.  Arguments and
+ * results are those of cosma_gpu_dgemm_ozaki_device (same kernels, same
+ * output bits); the caller still provides A, B and C in device memory.
+ * Scratch comes from one static device array of
+ * COSMA_GPU_OZAKI_NOALLOC_SCRATCH_BYTES; problems needing more are rejected
+ * with COSMA_GPU_ERROR_INVALID_ARGUMENT and a message giving the size (about
+ * m = n = k = 1024 with 13 slices fits).  The first call on each device looks
+ * up the array's device address, so make it before any stream capture.  All
+ * calls share the one array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller. */
+int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                  double alpha, const double* A, int64_t lda, const double* B,
+                                  int64_t ldb, double beta, double* C, int64_t ldc, int slices,
+                                  void* stream, cosma_gpu_ozaki_info* info);
+
 /* ------------------------------------- COSTA 1x1-grid layout transforms */
 /* dst(rows x cols) = op(src) where op in {'N','T','C'}: the block-cyclic ->
  * COSMA-blocked pack that costa::transformer::schedule(scalapack -> cosma,
