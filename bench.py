@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--phi", type=int, default=0)
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison run")
     p.add_argument("--no-variants", action="store_true", help="skip the phi = 8 / 32 variants")
+    p.add_argument("--config", default="precision", choices=["precision", "pdgemm"],
+                   help="precision: the headline line; pdgemm: the 1x1 ScaLAPACK configuration")
     return p.parse_args()
 
 
@@ -164,10 +166,114 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_pdgemm(args):
+    """pdgemm on a 1x1 grid: C = 1.5 * A^T * B + 0.5 * C, m = n = 4096, k = 65536,
+    128 x 128 blocks, N(0,1) entries.  Device phases (COSTA pack of A with
+    transpose, pack of B, GEMM, alpha/beta unpack) are timed with CUDA events on
+    the launching stream; e2e is the pdgemm_ symbol called with host arrays."""
+    import torch
+
+    import cosma_gb300 as cg
+    import oracle
+
+    dev = torch.device("cuda", 0)
+    m = n = 4096
+    k = 65536
+    alpha, beta = 1.5, 0.5
+    A = oracle.normal((k, m), 1)  # stored k x m, op(A) = A^T
+    B = oracle.normal((k, n), 2)
+    C0 = oracle.normal((m, n), 3)
+    dAsc = torch.from_numpy(A.reshape(-1, order="F")).to(dev)
+    dBsc = torch.from_numpy(B.reshape(-1, order="F")).to(dev)
+    dCsc = torch.from_numpy(C0.reshape(-1, order="F")).to(dev)
+    dA = torch.empty(m * k, dtype=torch.float64, device=dev)
+    dB = torch.empty(k * n, dtype=torch.float64, device=dev)
+    dCc = torch.empty(m * n, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream(dev)
+    method = "ozaki"
+
+    def phases():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        ev[0].record(s)
+        cg.pack("T", m, k, dAsc, k, dA, m, stream=s)
+        ev[1].record(s)
+        cg.pack("N", k, n, dBsc, k, dB, k, stream=s)
+        ev[2].record(s)
+        if method == "ozaki":
+            cg.dgemm_ozaki_device("N", "N", m, n, k, 1.0, dA, m, dB, k, 0.0, dCc, m, stream=s)
+        else:
+            cg.gemm_device("N", "N", m, n, k, 1.0, dA, m, dB, k, 0.0, dCc, m, method=method, stream=s)
+        ev[3].record(s)
+        cg.unpack(m, n, alpha, dCc, m, beta, dCsc, m, stream=s)
+        ev[4].record(s)
+        torch.cuda.synchronize()
+        return [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+
+    for _ in range(max(args.warmup, 3)):
+        dCsc.copy_(torch.from_numpy(C0.reshape(-1, order="F")))
+        phases()
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    times = []
+    for _ in range(args.steps):
+        times.append(phases())
+    clocks = sampler.stop()
+    t = np.median(np.array(times), axis=0)
+    total = float(t.sum())
+    flops = 2.0 * m * n * k
+    pk, pk_kind = peaks()
+    pack_a_bytes = 2.0 * m * k * 8
+    pack_b_bytes = 2.0 * k * n * 8
+    unpack_bytes = 3.0 * m * n * 8
+    gbs = lambda b, ms: b / (ms * 1e-3) / 1e9
+    # e2e: the ScaLAPACK symbol with host arrays
+    desca = cg.descinit(k, m, 128, 128, 0, 0, 0, k)
+    descb = cg.descinit(k, n, 128, 128, 0, 0, 0, k)
+    descc = cg.descinit(m, n, 128, 128, 0, 0, 0, m)
+    cg.pxgemm_set_method(method)
+    Ch = C0.copy(order="F")
+    cg.pxgemm("T", "N", m, n, k, alpha, A, 1, 1, desca, B, 1, 1, descb, beta, Ch, 1, 1, descc)
+    e2e = []
+    for _ in range(max(1, min(args.steps, 3))):
+        Ch = C0.copy(order="F")
+        t0 = time.perf_counter()
+        cg.pxgemm("T", "N", m, n, k, alpha, A, 1, 1, desca, B, 1, 1, descb, beta, Ch, 1, 1, descc)
+        e2e.append(time.perf_counter() - t0)
+    cg.pxgemm_set_method("native")
+    e2e_s = float(np.median(e2e))
+    # accuracy of the host result on sampled entries (double-double oracle)
+    rng = np.random.default_rng(7)
+    rows, cols = rng.integers(0, m, 1024), rng.integers(0, n, 1024)
+    hi, lo, ab = oracle.gemm_dd_sampled("T", "N", A, B, rows, cols)
+    exact = alpha * (hi + lo) + beta * C0[rows, cols]
+    rel = np.abs(Ch[rows, cols] - exact) / np.maximum(np.abs(exact), 1e-300)
+    out = {"metric": "pdgemm 1x1 TFLOP/s (COSTA pack + FP64-accurate GEMM + unpack)",
+           "value": flops / (total * 1e-3) / 1e12, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": total, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic N(0,1), seeded",
+           "config": {"workload": "pdgemm 1x1 grid C = 1.5*A^T*B + 0.5*C, m=n=4096, k=65536, 128x128 blocks",
+                      "gemm_method": method},
+           "phases_ms": {"pack_A_transpose": t[0], "pack_B": t[1], "gemm": t[2], "unpack_alpha_beta": t[3]},
+           "pack_GBs": {"A_transpose": gbs(pack_a_bytes, t[0]), "B_copy": gbs(pack_b_bytes, t[1]),
+                        "unpack": gbs(unpack_bytes, t[3])},
+           "roofline": {"bound": "hbm", "achieved": gbs(pack_a_bytes, t[0]), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                        "frac": gbs(pack_a_bytes, t[0]) / pk["hbm_gbs"], "traffic": None,
+                        "kernel": "transpose_kernel (COSTA pack, op T)", "peak_note": pk_kind},
+           "accuracy": {"max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()), "samples": 1024},
+           "e2e": {"value": flops / e2e_s / 1e12, "unit": UNIT, "h2d_bytes_per_step": (m * k + k * n + m * n) * 8,
+                   "d2h_bytes_per_step": m * n * 8, "entry": "pdgemm_ (ScaLAPACK symbol), host arrays",
+                   "ms_per_step": e2e_s * 1e3},
+           "clocks": clocks, "gpu_launches": 4 * args.steps}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "pdgemm":
+        return run_pdgemm(args)
     import torch
 
     import cosma_gb300 as cg

@@ -470,6 +470,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int quad = warp & 3;  // TMEM lanes this warp may access
         const int row = quad * 32 + lane;
         ulonglong2* W = p.W + (size_t)blockIdx.x * (BM * BN);
+        const uint64_t pol_keep = tc::policy_evict_last(), pol_stream = tc::policy_evict_first();
         uint32_t acc_it = 0;
         bool ok = true;
         const int last = sc.n_groups - 1;
@@ -489,21 +490,28 @@ __global__ void __launch_bounds__(THREADS, 1)
                 for (int c = 0; c < BN / 32; ++c) {
                     uint32_t v[32];
                     tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + buf * BN + c * 32, v);
+                    // the partial sums of this chunk are requested all at once, and kept
+                    // at the back of the L2 eviction order: between two drains of a tile
+                    // they must survive the operand tiles streaming through L2
+                    ulonglong2 w[32];
+                    ulonglong2* wp = W + (c * 32) * BM + row;
+                    if (g > 0) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) w[j] = tc::ld_u128_hint(wp + j * BM, pol_keep);
+                    }
                     tc::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int col = c * 32 + j;
                         const int x = __float2int_rn(__uint_as_float(v[j]));
-                        ulonglong2* wp = W + col * BM + row;
                         unsigned long long lo = 0, hi = 0;
                         if (g > 0) {
-                            const ulonglong2 w = *wp;
-                            lo = w.x;
-                            hi = w.y;
+                            lo = w[j].x;
+                            hi = w[j].y;
                         }
                         add_shifted(lo, hi, x, sh);
                         if (g < last) {
-                            *wp = make_ulonglong2(lo, hi);
+                            tc::st_u128_hint(wp + j * BM, make_ulonglong2(lo, hi), pol_keep);
                         } else {
                             const int64_t gj = (int64_t)nb * BN + col;
                             if (gi < p.m && gj < p.n) {
@@ -512,7 +520,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 // C = fl(fl(alpha*r) + fl(beta*C)), no contraction
                                 if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
                                 if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
-                                *cp = r;
+                                tc::st_f64_hint(cp, r, pol_stream);
                             }
                         }
                     }
