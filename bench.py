@@ -46,8 +46,9 @@ def parse():
     p.add_argument("--phi", type=int, default=0)
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison run")
     p.add_argument("--no-variants", action="store_true", help="skip the phi = 8 / 32 variants")
-    p.add_argument("--config", default="precision", choices=["precision", "pdgemm"],
-                   help="precision: the headline line; pdgemm: the 1x1 ScaLAPACK configuration")
+    p.add_argument("--config", default="precision", choices=["precision", "pdgemm", "sgemm"],
+                   help="precision: the headline line; pdgemm: the 1x1 ScaLAPACK configuration; "
+                        "sgemm: the FP32 3xBF16 variant of the precision configuration")
     return p.parse_args()
 
 
@@ -268,12 +269,86 @@ def run_pdgemm(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sgemm(args):
+    """FP32 GEMM m = n = k = 16384, N(0,1) entries, through the 3xBF16 path;
+    cuBLAS SGEMM (FP32 SIMT, TF32 off) timed beside it for context."""
+    import torch
+
+    import cosma_gb300 as cg
+    import oracle
+
+    dev = torch.device("cuda", 0)
+    n = args.size
+    A = oracle.normal((n, n), 1, dtype=np.float32)
+    B = oracle.normal((n, n), 2, dtype=np.float32)
+    dA = torch.from_numpy(A.reshape(-1, order="F")).to(dev)
+    dB = torch.from_numpy(B.reshape(-1, order="F")).to(dev)
+    dC = torch.empty(n * n, dtype=torch.float32, device=dev)
+    s = torch.cuda.current_stream(dev)
+
+    def step():
+        cg.gemm_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, method="bf16x3", stream=s, scalar="s")
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = 2.0 * n * n * n
+    rng = np.random.default_rng(5)
+    rows, cols = rng.integers(0, n, 2048), rng.integers(0, n, 2048)
+    Cg = dC.cpu().numpy().reshape(n, n).T
+    exact = np.einsum("ij,ji->i", A[rows, :].astype(np.float64), B[:, cols].astype(np.float64))
+    absab = np.einsum("ij,ji->i", np.abs(A[rows, :]).astype(np.float64), np.abs(B[:, cols]).astype(np.float64))
+    err = np.abs(Cg[rows, cols] - exact)
+    # cuBLAS SGEMM on the same data (row-major view: C^T = B^T A^T)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    At = dA.view(n, n)  # = A^T row-major
+    Bt = dB.view(n, n)
+    Ct = torch.matmul(Bt, At)
+    torch.cuda.synchronize()
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record()
+    Ct = torch.matmul(Bt, At)
+    c1.record()
+    torch.cuda.synchronize()
+    cublas_ms = c0.elapsed_time(c1)
+    Cc = Ct.cpu().numpy().T  # column-major C
+    err_cublas = np.abs(Cc[rows, cols] - exact)
+    pk, pk_kind = peaks()
+    out = {"metric": "FP32 GEMM TFLOP/s (3xBF16 split on BF16 tensor cores)", "value": flops / (ms * 1e-3) / 1e12,
+           "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic N(0,1), seeded",
+           "config": {"workload": f"precision: SGEMM NN m=n=k={n}, N(0,1), 3xBF16 (6 BF16 products)"},
+           "accuracy": {"max_err_over_absab": float((err / absab).max()), "max_abs_err": float(err.max()),
+                        "cublas_sgemm_max_err_over_absab": float((err_cublas / absab).max())},
+           "cublas_sgemm_tflops": flops / (cublas_ms * 1e-3) / 1e12,
+           "roofline": {"bound": "tensor", "achieved": 6 * flops / (ms * 1e-3) / 1e12, "peak": pk["bf16_tflops"],
+                        "unit": "TFLOP/s", "frac": 6 * flops / (ms * 1e-3) / 1e12 / pk["bf16_tflops"],
+                        "traffic": None, "kernel": "bf16x3_gemm_kernel (tcgen05 kind::f16), step incl. slicing",
+                        "peak_note": f"{pk_kind} BF16 burst"},
+           "clocks": clocks, "gpu_launches": 3 * args.steps}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.config == "pdgemm":
         return run_pdgemm(args)
+    if args.config == "sgemm":
+        return run_sgemm(args)
     import torch
 
     import cosma_gb300 as cg

@@ -38,7 +38,11 @@ int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t st
         return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: leading dimension too small");
     // k == 0 or alpha == 0: C <- beta * C (cosma_pxgemm.cpp:41-46 semantics)
     if (g.k == 0 || is_zero(g.alpha, g.scalar)) return scale_matrix_device(g.scalar, g.m, g.n, g.beta, g.C, g.ldc, stream);
-    if (method == COSMA_GPU_METHOD_AUTO) method = COSMA_GPU_METHOD_NATIVE;
+    // AUTO: the reference's native arithmetic, except for real single precision,
+    // which runs 3xBF16 on the tensor cores (FP32 accuracy; the FP64 pipe that the
+    // native kernel uses for FP32 inputs is ~60x slower on GB300).
+    if (method == COSMA_GPU_METHOD_AUTO)
+        method = g.scalar == Scalar::S ? COSMA_GPU_METHOD_BF16X3 : COSMA_GPU_METHOD_NATIVE;
     if (method == COSMA_GPU_METHOD_OZAKI) {
         if (g.scalar == Scalar::D) return ozaki_dgemm(g, ozaki_slices, stream, info);
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "gemm: the Ozaki method is implemented for double");
