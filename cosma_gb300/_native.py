@@ -30,6 +30,21 @@ class OzakiInfo(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class GemmProblem(C.Structure):
+    _fields_ = [("transa", C.c_char), ("transb", C.c_char), ("m", C.c_int32), ("n", C.c_int32), ("k", C.c_int32),
+                ("alpha", C.c_double), ("beta", C.c_double), ("A", C.c_void_p), ("lda", C.c_int64),
+                ("B", C.c_void_p), ("ldb", C.c_int64), ("C", C.c_void_p), ("ldc", C.c_int64)]
+
+
+class GroupedInfo(C.Structure):
+    _fields_ = [("tiles", C.c_int), ("tile_policy", C.c_int), ("dynamic_schedule", C.c_int),
+                ("warps_per_cta", C.c_int), ("useful_flops", C.c_double), ("padded_flops", C.c_double),
+                ("tuned_ms", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 i32, i64, dbl, flt, vp, ch = C.c_int, C.c_int64, C.c_double, C.c_float, C.c_void_p, C.c_char
 _PX = [vp] * 19
 
@@ -59,6 +74,11 @@ SIGNATURES = {
                                            C.POINTER(OzakiInfo)]),
     "cosma_gpu_dgemm_ozaki_noalloc": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                             C.POINTER(OzakiInfo)]),
+    "cosma_gpu_grouped_plan_create": (vp, [i32, i32, C.POINTER(GemmProblem), i32, vp]),
+    "cosma_gpu_grouped_plan_run": (i32, [vp, vp]),
+    "cosma_gpu_grouped_plan_info": (i32, [vp, C.POINTER(GroupedInfo)]),
+    "cosma_gpu_grouped_plan_destroy": (None, [vp]),
+    "cosma_gpu_dgemm_grouped_device": (i32, [i32, i32, C.POINTER(GemmProblem), vp]),
     "costa_gpu_pack": (i32, [ch, i32, i32, i64, i64, vp, i64, vp, i64, vp]),
     "costa_gpu_unpack_d": (i32, [i64, i64, dbl, vp, i64, dbl, vp, i64, vp]),
     "costa_gpu_unpack_s": (i32, [i64, i64, flt, vp, i64, flt, vp, i64, vp]),

@@ -197,6 +197,43 @@ def dgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm,
     return info.as_dict()
 
 
+class GroupedPlan:
+    """A grouped FP64 GEMM over many device problems, one persistent launch
+    replayed from a CUDA graph.  `problems` is a list of tuples
+    (transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) with device
+    buffers (torch tensors or raw addresses)."""
+
+    def __init__(self, problems, method="native", autotune=True, stream=None):
+        self.lib = N.load()
+        arr = (N.GemmProblem * max(1, len(problems)))()
+        for i, (ta, tb, m, n, k, al, A, lda, B, ldb, be, Cm, ldc) in enumerate(problems):
+            arr[i] = N.GemmProblem(ta.encode(), tb.encode(), m, n, k, al, be, ptr(A), lda, ptr(B), ldb, ptr(Cm), ldc)
+        self._keep = problems  # the device buffers must outlive the plan
+        meth = N.METHODS[method] if isinstance(method, str) else int(method)
+        self._p = self.lib.cosma_gpu_grouped_plan_create(meth, len(problems), arr, int(autotune), _stream_ptr(stream))
+        if not self._p:
+            N.check(self.lib.cosma_gpu_last_error() or 6)
+
+    def run(self, stream=None):
+        N.check(self.lib.cosma_gpu_grouped_plan_run(self._p, _stream_ptr(stream)))
+
+    def info(self):
+        inf = N.GroupedInfo()
+        N.check(self.lib.cosma_gpu_grouped_plan_info(self._p, C.byref(inf)))
+        return inf.as_dict()
+
+    def close(self):
+        if self._p:
+            self.lib.cosma_gpu_grouped_plan_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def pack(op, rows, cols, src, ld_src, dst, ld_dst, is_complex=False, elem_bytes=8, stream=None):
     """COSTA 1x1 pack: dst(rows x cols) = op(src) on CUDA buffers."""
     lib = N.load()

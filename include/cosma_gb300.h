@@ -177,6 +177,51 @@ int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m, int64_t n
                                   int64_t ldb, double beta, double* C, int64_t ldc, int slices,
                                   void* stream, cosma_gpu_ozaki_info* info);
 
+/* ------------------------------------------------- grouped (batched) GEMM */
+/* One problem of a batch: C = alpha * op(A) * op(B) + beta * C on device
+ * pointers (column-major).  Layout is part of the ABI (80 bytes). */
+typedef struct cosma_gpu_gemm_problem {
+    char transa, transb; /* 'N', 'T' or 'C' */
+    int32_t m, n, k;
+    double alpha, beta;
+    const double* A;
+    int64_t lda;
+    const double* B;
+    int64_t ldb;
+    double* C;
+    int64_t ldc;
+} cosma_gpu_gemm_problem;
+
+typedef struct cosma_gpu_grouped_info {
+    int tiles;            /* tiles in the persistent launch                  */
+    int tile_policy;      /* 0 all 32x32, 1 per-problem shapes, 2 16-row tiles for small m/n */
+    int dynamic_schedule; /* 1: warps fetch tiles through an atomic counter  */
+    int warps_per_cta;
+    double useful_flops;  /* sum of 2 m n k                                  */
+    double padded_flops;  /* work the tiles actually issue                   */
+    double tuned_ms;      /* time of the chosen configuration while tuning   */
+} cosma_gpu_grouped_info;
+
+/* A grouped GEMM of `count` independent FP64 problems in one persistent
+ * launch, captured in a CUDA graph.  The reference runs such batches as a loop
+ * of local_multiply calls (src/cosma/multiply.cpp:476-587); there is no
+ * grouped entry point in the reference.  With autotune != 0 the tile policy,
+ * schedule and CTA size are chosen by timing candidates on the batch (the
+ * choice is cached per batch signature); tuning runs the batch several times
+ * and restores the C of problems with beta != 0.  The problem array is copied;
+ * the device buffers must stay valid while the plan is used. */
+typedef struct cosma_gpu_grouped_plan cosma_gpu_grouped_plan;
+cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count,
+                                                      const cosma_gpu_gemm_problem* problems,
+                                                      int autotune, void* stream);
+/* Replays the plan's CUDA graph on `stream` (asynchronous). */
+int cosma_gpu_grouped_plan_run(cosma_gpu_grouped_plan* plan, void* stream);
+int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* plan, cosma_gpu_grouped_info* info);
+void cosma_gpu_grouped_plan_destroy(cosma_gpu_grouped_plan* plan);
+/* One-shot grouped GEMM (plan without tuning, run, synchronise, destroy). */
+int cosma_gpu_dgemm_grouped_device(int method, int count, const cosma_gpu_gemm_problem* problems,
+                                   void* stream);
+
 /* ------------------------------------- COSTA 1x1-grid layout transforms */
 /* dst(rows x cols) = op(src) where op in {'N','T','C'}: the block-cyclic ->
  * COSMA-blocked pack that costa::transformer::schedule(scalapack -> cosma,
