@@ -78,6 +78,12 @@ class MMHandle:
         N.check(self.lib.cosma_gpu_tmm_last_ozaki_info(self._h, C.byref(info)))
         return info.as_dict()
 
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes moved by the last gemm call."""
+        h2d, d2h = C.c_int64(), C.c_int64()
+        N.check(self.lib.cosma_gpu_tmm_last_transfer_bytes(self._h, C.byref(h2d), C.byref(d2h)))
+        return h2d.value, d2h.value
+
     def device_buffer_c(self) -> int:
         return self.lib.cosma_gpu_tmm_device_buffer_c(self._h) or 0
 

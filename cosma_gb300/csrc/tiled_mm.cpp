@@ -46,7 +46,9 @@ struct cosma_gpu_mm_handle {
     void* last_device_c = nullptr;
     std::map<uintptr_t, size_t> pinned;  // registered host ranges (base -> bytes)
     std::mutex mu;
-    cosma_gpu_ozaki_info last_info{0, 0, 0, 0, 0.0};
+    cosma_gpu_ozaki_info last_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    int64_t last_h2d_bytes = 0, last_d2h_bytes = 0;
+    cudaEvent_t ev_ready[2] = {}, ev_free[2] = {}, ev_cin[2] = {}, ev_cdone[2] = {}, ev_cout[2] = {};
 };
 
 namespace cgb {
@@ -132,9 +134,13 @@ int handle_init(cosma_gpu_mm_handle* h) {
     CGB_CUDA(cudaGetDevice(&h->device));
     h->streams.resize(h->n_streams);
     for (auto& s : h->streams) CGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    h->bufA.resize(h->n_streams);
-    h->bufB.resize(h->n_streams);
-    h->bufC.resize(h->n_streams);
+    // two operand slots and two C slots (sized once: DeviceBuffer is not movable)
+    h->bufA.resize(2);
+    h->bufB.resize(2);
+    h->bufC.resize(2);
+    for (int i = 0; i < 2; ++i)
+        for (cudaEvent_t* e : {&h->ev_ready[i], &h->ev_free[i], &h->ev_cin[i], &h->ev_cdone[i], &h->ev_cout[i]})
+            CGB_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     return COSMA_GPU_SUCCESS;
 }
 
@@ -187,121 +193,165 @@ int tmm_gemm(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int64_t m, int
     return status;
 }
 
-// The tile loop of tmm_gemm (host or mixed pointers).
+// The host<->HBM streamer behind tmm_gemm (host or mixed pointers).
+//
+// Work is a sequence of steps (C tile, K slab).  Three streams play fixed
+// roles - H2D copies, GEMMs, D2H copies - and two rings of device buffers
+// (operand slots for A/B slabs, C slots for C tiles) are chained with events:
+// the copies of step i+1 are enqueued before the GEMM of step i is called, so
+// they run while it computes even when the GEMM call itself blocks the host
+// (the Ozaki path reads its slice statistics back), and the D2H of a finished
+// C tile overlaps the next tile.  Tiles never exceed the handle's limits and
+// shrink until the rings fit in 60% of free HBM.
 int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int opa, int opb, int64_t m, int64_t n,
                      int64_t k, const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
                      const double* beta, void* C, int64_t ldc, bool dA, bool dB, bool dC, bool trivial,
                      bool copy_c_back, cosma_gpu_ozaki_info* info) {
     const size_t es = scalar_bytes(sc);
-
-    // Tile plan: tiles never exceed the handle's limits; shrink the largest
-    // dimension until the per-stream buffers fit in 60% of free HBM.
+    constexpr int R = 2;  // operand slots and C slots
     int64_t tm = std::min<int64_t>(m, h->tile_m), tn = std::min<int64_t>(n, h->tile_n);
     int64_t tk = std::min<int64_t>(std::max<int64_t>(k, 1), h->tile_k);
     size_t free_b = 0, total_b = 0;
     CGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const int S = h->n_streams;
+    size_t have = 0;
+    for (int s = 0; s < R; ++s) have += h->bufA[s].bytes + h->bufB[s].bytes + h->bufC[s].bytes;
     for (;;) {
-        size_t per = ((dA ? 0 : (size_t)tm * tk) + (dB ? 0 : (size_t)tk * tn) + (dC ? 0 : (size_t)tm * tn)) * es;
-        size_t have = 0;
-        for (int s = 0; s < S; ++s) have += h->bufA[s].bytes + h->bufB[s].bytes + h->bufC[s].bytes;
-        if (per * S <= (size_t)(0.6 * (double)(free_b + have)) || (tm <= 256 && tn <= 256 && tk <= 256)) break;
+        const size_t per = (R * ((dA || trivial ? 0 : (size_t)tm * tk) + (dB || trivial ? 0 : (size_t)tk * tn)) +
+                            R * (dC ? 0 : (size_t)tm * tn)) * es;
+        if (per <= (size_t)(0.6 * (double)(free_b + have)) || (tm <= 256 && tn <= 256 && tk <= 256)) break;
         if (tk >= tm && tk >= tn) tk = (tk + 1) / 2;
         else if (tm >= tn) tm = (tm + 1) / 2;
         else tn = (tn + 1) / 2;
     }
-    const int64_t ntm = ceil_div(m, tm), ntn = ceil_div(n, tn), ntk = trivial ? 0 : ceil_div(k, tk);
-    const int64_t ntiles = ntm * ntn;
-    const int used_streams = (int)std::min<int64_t>(S, ntiles);
-    for (int s = 0; s < used_streams; ++s) {
-        if (!dA && !trivial) CGB_CHECK(h->bufA[s].reserve((size_t)tm * tk * es, h->streams[s]));
-        if (!dB && !trivial) CGB_CHECK(h->bufB[s].reserve((size_t)tk * tn * es, h->streams[s]));
-        if (!dC) CGB_CHECK(h->bufC[s].reserve((size_t)tm * tn * es, h->streams[s]));
+    const int64_t ntm = ceil_div(m, tm), ntn = ceil_div(n, tn), ntk = trivial ? 1 : ceil_div(k, tk);
+    const int64_t ntiles = ntm * ntn, nsteps = ntiles * ntk;
+    for (int s = 0; s < R; ++s) {
+        if (!dA && !trivial) CGB_CHECK(h->bufA[s].reserve((size_t)tm * tk * es, h->streams[0]));
+        if (!dB && !trivial) CGB_CHECK(h->bufB[s].reserve((size_t)tk * tn * es, h->streams[0]));
+        if (!dC) CGB_CHECK(h->bufC[s].reserve((size_t)tm * tn * es, h->streams[0]));
     }
     const bool keep_on_device = !dC && !copy_c_back;
     if (keep_on_device) CGB_CHECK(h->full_c.reserve((size_t)m * n * es, h->streams[0]));
     CGB_CUDA(cudaDeviceSynchronize());  // buffers from any earlier call are idle
 
+    const int S = (int)h->streams.size();
+    cudaStream_t cs = h->streams[0], hs = h->streams[std::min(1, S - 1)], ds = h->streams[std::min(2, S - 1)];
+    cudaEvent_t* ev_ready = h->ev_ready;    // operand slot filled
+    cudaEvent_t* ev_free = h->ev_free;      // operand slot read by its GEMM
+    cudaEvent_t* ev_cin = h->ev_cin;        // C slot filled (beta != 0) / free to overwrite
+    cudaEvent_t* ev_cdone = h->ev_cdone;    // C slot final
+    cudaEvent_t* ev_cout = h->ev_cout;      // C slot drained to its destination
+    bool slot_used[R] = {false, false}, cslot_used[R] = {false, false};
+    h->last_h2d_bytes = 0;
+    h->last_d2h_bytes = 0;
     const double one[2] = {1.0, 0.0};
-    int status = COSMA_GPU_SUCCESS;
-    for (int64_t t = 0; t < ntiles && status == COSMA_GPU_SUCCESS; ++t) {
-        const int s_idx = (int)(t % used_streams);
-        cudaStream_t st = h->streams[s_idx];
+    const bool beta_zero = is_zero(beta, sc);
+
+    auto tile_of = [&](int64_t step, int64_t& i0, int64_t& j0, int64_t& mi, int64_t& nj, int64_t& l0, int64_t& kk) {
+        const int64_t t = step / ntk, kt = step % ntk;
         const int64_t ti = t % ntm, tj = t / ntm;
-        const int64_t i0 = ti * tm, j0 = tj * tn;
-        const int64_t mi = std::min(tm, m - i0), nj = std::min(tn, n - j0);
-        // C tile
-        char* cdev;
+        i0 = ti * tm; j0 = tj * tn;
+        mi = std::min(tm, m - i0); nj = std::min(tn, n - j0);
+        l0 = kt * tk; kk = trivial ? 0 : std::min(tk, k - l0);
+    };
+    auto cdev_of = [&](int64_t step, int64_t i0, int64_t j0, int64_t& cld) -> char* {
+        if (dC) { cld = ldc; return (char*)C + (i0 + j0 * ldc) * es; }
+        const int64_t t = step / ntk;
+        int64_t mi = std::min(tm, m - i0);
+        cld = mi;
+        return (char*)h->bufC[t % R].ptr;
+    };
+    // device pointers of the op(A) / op(B) slabs of a step (issuing the H2D copies when host-resident)
+    auto issue_copies = [&](int64_t step) -> int {
+        int64_t i0, j0, mi, nj, l0, kk;
+        tile_of(step, i0, j0, mi, nj, l0, kk);
+        const int r = (int)(step % R);
+        const int64_t t = step / ntk, kt = step % ntk;
+        const int c = (int)(t % R);
+        if (kt == 0 && !dC && !beta_zero) {  // C tile comes in once, before its first K slab
+            if (cslot_used[c]) CGB_CUDA(cudaStreamWaitEvent(hs, ev_cout[c], 0));
+            CGB_CHECK(copy2d(h->bufC[c].ptr, mi, (const char*)C + (i0 + j0 * ldc) * es, ldc, mi, nj, es,
+                             cudaMemcpyHostToDevice, hs));
+            h->last_h2d_bytes += mi * nj * es;
+            CGB_CUDA(cudaEventRecord(ev_cin[c], hs));
+        }
+        if (trivial) return COSMA_GPU_SUCCESS;
+        if (slot_used[r] && (!dA || !dB)) CGB_CUDA(cudaStreamWaitEvent(hs, ev_free[r], 0));
+        if (!dA) {
+            if (opa == 0) CGB_CHECK(copy2d(h->bufA[r].ptr, mi, (const char*)A + (i0 + l0 * lda) * es, lda, mi, kk, es,
+                                           cudaMemcpyHostToDevice, hs));
+            else CGB_CHECK(copy2d(h->bufA[r].ptr, kk, (const char*)A + (l0 + i0 * lda) * es, lda, kk, mi, es,
+                                  cudaMemcpyHostToDevice, hs));
+            h->last_h2d_bytes += mi * kk * es;
+        }
+        if (!dB) {
+            if (opb == 0) CGB_CHECK(copy2d(h->bufB[r].ptr, kk, (const char*)B + (l0 + j0 * ldb) * es, ldb, kk, nj, es,
+                                           cudaMemcpyHostToDevice, hs));
+            else CGB_CHECK(copy2d(h->bufB[r].ptr, nj, (const char*)B + (j0 + l0 * ldb) * es, ldb, nj, kk, es,
+                                  cudaMemcpyHostToDevice, hs));
+            h->last_h2d_bytes += kk * nj * es;
+        }
+        CGB_CUDA(cudaEventRecord(ev_ready[r], hs));
+        slot_used[r] = true;
+        return COSMA_GPU_SUCCESS;
+    };
+    auto compute = [&](int64_t step) -> int {
+        int64_t i0, j0, mi, nj, l0, kk;
+        tile_of(step, i0, j0, mi, nj, l0, kk);
+        const int r = (int)(step % R);
+        const int64_t t = step / ntk, kt = step % ntk;
+        const int c = (int)(t % R);
         int64_t cld;
-        if (dC) {
-            cdev = (char*)C + (i0 + j0 * ldc) * es;
-            cld = ldc;
-        } else {
-            cdev = (char*)h->bufC[s_idx].ptr;
-            cld = mi;
-            if (!is_zero(beta, sc))
-                if ((status = copy2d(cdev, cld, (const char*)C + (i0 + j0 * ldc) * es, ldc, mi, nj, es,
-                                     cudaMemcpyHostToDevice, st)))
-                    break;
+        char* cdev = cdev_of(step, i0, j0, cld);
+        if (kt == 0 && !dC) {
+            if (!beta_zero) CGB_CUDA(cudaStreamWaitEvent(cs, ev_cin[c], 0));
+            else if (cslot_used[c]) CGB_CUDA(cudaStreamWaitEvent(cs, ev_cout[c], 0));  // slot drained before overwrite
         }
         if (trivial) {
-            status = scale_matrix_device(sc, mi, nj, beta, cdev, cld, st);
-        }
-        for (int64_t kt = 0; kt < ntk && status == COSMA_GPU_SUCCESS; ++kt) {
-            const int64_t l0 = kt * tk, kk = std::min(tk, k - l0);
-            // op(A) tile rows [i0, i0+mi) x cols [l0, l0+kk)
+            CGB_CHECK(scale_matrix_device(sc, mi, nj, beta, cdev, cld, cs));
+        } else {
+            if (!dA || !dB) CGB_CUDA(cudaStreamWaitEvent(cs, ev_ready[r], 0));
             const char* adev;
             int64_t ald;
-            if (opa == 0) {
-                const char* src = (const char*)A + (i0 + l0 * lda) * es;
-                if (dA) { adev = src; ald = lda; }
-                else {
-                    adev = (const char*)h->bufA[s_idx].ptr; ald = mi;
-                    if ((status = copy2d((void*)adev, ald, src, lda, mi, kk, es, cudaMemcpyHostToDevice, st))) break;
-                }
-            } else {
-                const char* src = (const char*)A + (l0 + i0 * lda) * es;
-                if (dA) { adev = src; ald = lda; }
-                else {
-                    adev = (const char*)h->bufA[s_idx].ptr; ald = kk;
-                    if ((status = copy2d((void*)adev, ald, src, lda, kk, mi, es, cudaMemcpyHostToDevice, st))) break;
-                }
-            }
-            // op(B) tile rows [l0, l0+kk) x cols [j0, j0+nj)
+            if (dA) { adev = (const char*)A + (opa == 0 ? (i0 + l0 * lda) : (l0 + i0 * lda)) * es; ald = lda; }
+            else { adev = (const char*)h->bufA[r].ptr; ald = opa == 0 ? mi : kk; }
             const char* bdev;
             int64_t bld;
-            if (opb == 0) {
-                const char* src = (const char*)B + (l0 + j0 * ldb) * es;
-                if (dB) { bdev = src; bld = ldb; }
-                else {
-                    bdev = (const char*)h->bufB[s_idx].ptr; bld = kk;
-                    if ((status = copy2d((void*)bdev, bld, src, ldb, kk, nj, es, cudaMemcpyHostToDevice, st))) break;
-                }
-            } else {
-                const char* src = (const char*)B + (j0 + l0 * ldb) * es;
-                if (dB) { bdev = src; bld = ldb; }
-                else {
-                    bdev = (const char*)h->bufB[s_idx].ptr; bld = nj;
-                    if ((status = copy2d((void*)bdev, bld, src, ldb, nj, kk, es, cudaMemcpyHostToDevice, st))) break;
-                }
-            }
+            if (dB) { bdev = (const char*)B + (opb == 0 ? (l0 + j0 * ldb) : (j0 + l0 * ldb)) * es; bld = ldb; }
+            else { bdev = (const char*)h->bufB[r].ptr; bld = opb == 0 ? kk : nj; }
             GemmDesc g = make_gemm_desc(sc, ta, tb, mi, nj, kk, alpha, adev, ald, bdev, bld, kt == 0 ? beta : one,
                                         cdev, cld);
             cosma_gpu_ozaki_info ti_info;
-            status = gemm_device(g, h->method, h->slices, st, &ti_info);
+            CGB_CHECK(gemm_device(g, h->method, h->slices, cs, &ti_info));
             if (ti_info.slices) *info = ti_info;
+            CGB_CUDA(cudaEventRecord(ev_free[r], cs));
         }
-        if (status) break;
-        if (!dC) {
-            if (keep_on_device)
-                status = copy2d((char*)h->full_c.ptr + (i0 + j0 * m) * es, m, cdev, cld, mi, nj, es,
-                                cudaMemcpyDeviceToDevice, st);
-            else
-                status = copy2d((char*)C + (i0 + j0 * ldc) * es, ldc, cdev, cld, mi, nj, es, cudaMemcpyDeviceToHost, st);
+        if (kt == ntk - 1 && !dC) {  // tile final: drain it on the D2H stream
+            CGB_CUDA(cudaEventRecord(ev_cdone[c], cs));
+            CGB_CUDA(cudaStreamWaitEvent(ds, ev_cdone[c], 0));
+            if (keep_on_device) {
+                CGB_CHECK(copy2d((char*)h->full_c.ptr + (i0 + j0 * m) * es, m, cdev, cld, mi, nj, es,
+                                 cudaMemcpyDeviceToDevice, ds));
+            } else {
+                CGB_CHECK(copy2d((char*)C + (i0 + j0 * ldc) * es, ldc, cdev, cld, mi, nj, es, cudaMemcpyDeviceToHost,
+                                 ds));
+                h->last_d2h_bytes += mi * nj * es;
+            }
+            CGB_CUDA(cudaEventRecord(ev_cout[c], ds));
+            cslot_used[c] = true;
         }
+        return COSMA_GPU_SUCCESS;
+    };
+
+    int status = COSMA_GPU_SUCCESS;
+    for (int64_t i = 0; i < std::min<int64_t>(R - 1, nsteps) && status == COSMA_GPU_SUCCESS; ++i)
+        status = issue_copies(i);
+    for (int64_t i = 0; i < nsteps && status == COSMA_GPU_SUCCESS; ++i) {
+        if (i + R - 1 < nsteps) status = issue_copies(i + R - 1);
+        if (status == COSMA_GPU_SUCCESS) status = compute(i);
     }
-    for (int s = 0; s < used_streams; ++s) {
-        cudaError_t e = cudaStreamSynchronize(h->streams[s]);
+    for (cudaStream_t s : {cs, hs, ds}) {
+        cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess && status == COSMA_GPU_SUCCESS) status = cuda_status(e, "cudaStreamSynchronize");
     }
     h->last_device_c = dC ? C : (keep_on_device ? h->full_c.ptr : nullptr);
@@ -366,6 +416,9 @@ void cosma_gpu_tmm_destroy_context(cosma_gpu_mm_handle* h) {
         for (auto& kv : h->pinned) cudaHostUnregister((void*)kv.first);
         h->pinned.clear();
         for (auto s : h->streams) cudaStreamDestroy(s);
+        for (int i = 0; i < 2; ++i)
+            for (cudaEvent_t e : {h->ev_ready[i], h->ev_free[i], h->ev_cin[i], h->ev_cdone[i], h->ev_cout[i]})
+                if (e) cudaEventDestroy(e);
         cudaGetLastError();
     }
     delete h;
@@ -383,6 +436,14 @@ int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* h, int method, int slices) {
 }
 
 void* cosma_gpu_tmm_device_buffer_c(cosma_gpu_mm_handle* h) { return h ? h->last_device_c : nullptr; }
+
+int cosma_gpu_tmm_last_transfer_bytes(cosma_gpu_mm_handle* h, int64_t* h2d_bytes, int64_t* d2h_bytes) {
+    if (!h || !h2d_bytes || !d2h_bytes)
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "last_transfer_bytes: null argument");
+    *h2d_bytes = h->last_h2d_bytes;
+    *d2h_bytes = h->last_d2h_bytes;
+    return COSMA_GPU_SUCCESS;
+}
 
 int cosma_gpu_tmm_last_ozaki_info(cosma_gpu_mm_handle* h, cosma_gpu_ozaki_info* info) {
     if (!h || !info) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "last_ozaki_info: null argument");

@@ -81,6 +81,10 @@ int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* handle, int method, int ozaki_
 /* Device buffer holding the C of the last call made with copy_c_back == 0
  * (replaces mm_handle::get_full_device_buffer_c(), src/cosma/gpu/nccl_utils.cpp:200). */
 void* cosma_gpu_tmm_device_buffer_c(cosma_gpu_mm_handle* handle);
+/* Bytes the handle's last gemm call moved host->device and device->host
+ * (zero for operands that were already in device memory). */
+int cosma_gpu_tmm_last_transfer_bytes(cosma_gpu_mm_handle* handle, int64_t* h2d_bytes,
+                                      int64_t* d2h_bytes);
 /* Ozaki statistics of the handle's last call. */
 int cosma_gpu_tmm_last_ozaki_info(cosma_gpu_mm_handle* handle, cosma_gpu_ozaki_info* info);
 
