@@ -688,7 +688,7 @@ def main():
             traffic = None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": fp8_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp8_peak, "traffic": traffic,
-                "kernel": "ozaki_gemm_kernel (tcgen05 kind::f8f6f4)",
+                "kernel": "ozaki_gemm_pair_kernel (tcgen05.mma.cta_group::2 kind::f8f6f4, 256x256 tiles)",
                 "peak_note": f"FP8 dense peak taken as 2x the {pk_kind} BF16 burst figure "
                              f"({pk['bf16_tflops']} TFLOP/s)",
                 "kernel_ms": kms, "prep_ms": info["prep_ms"]}

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
             }
             const uint32_t first = it > STAGES ? it - STAGES : 0;
-            for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, p.err, 0);
+            for (uint32_t j = first; j < it; ++j) tc::mbar_wait_drain(&full[j % STAGES], (j / STAGES) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer: one accumulator per K chunk, buffers alternate
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
             }
             tc::mma_commit(drain);
-            tc::mbar_wait(drain, 0, p.err, 0);
+            tc::mbar_wait_drain(drain, 0);
         }
     } else {
         // Epilogue, 8 warps: two per TMEM lane quadrant, each owning 128 of the

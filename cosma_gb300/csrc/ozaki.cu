@@ -32,10 +32,13 @@
 // legacy warp-level IMMA path measured 151 TOP/s on GB300 against ~3.5
 // PFLOP/s for FP8, so the integer digits ride the FP8 pipe.
 //
-// GEMM kernel: persistent, warp-specialised; 128x256 output tile per CTA,
-// 128-byte-wide K blocks through a 4-stage TMA ring (48 KB/stage, 128-byte
-// swizzle), two 256-column FP32 accumulators in TMEM so that the epilogue of
-// one accumulator group overlaps the MMAs of the next.
+// GEMM kernels: persistent, warp-specialised; 128-byte-wide K blocks through
+// a 4-stage TMA ring (128-byte swizzle), two 256-column FP32 accumulators in
+// TMEM so that the epilogue of one accumulator group overlaps the MMAs of the
+// next.  Two forms: CTA pairs on 256 x 256 tiles (tcgen05 cta_group::2, 32 KB
+// per stage and CTA) whenever m spans two or more 128-row tiles, else single
+// CTAs on 128 x 256 tiles (48 KB per stage) in clusters along N that share
+// the A slab by TMA multicast.
 //   warp 0      TMA producer         warp 1   TMEM owner + MMA issuer
 //   warps 2..5  epilogue (TMEM -> registers -> 128-bit integer sums)
 #include "common.cuh"
@@ -63,6 +66,7 @@ constexpr int MAX_SLICES = 16;
 constexpr int MAX_UNITS = 144, MAX_GROUPS = 144;
 constexpr int64_t MAX_K_PER_CALL = 65536;  // 256 * k <= 2^24 for one product per accumulator
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int KB_CHUNK = 4;  // K blocks per chunk in the group loop (512 FP8 elements)
 
 struct Schedule {
     int n_groups;
@@ -355,14 +359,95 @@ __device__ __forceinline__ double i128_to_double(unsigned long long lo, unsigned
 // so every A- and B-slice panel a wave needs is fetched from HBM once and
 // served to the other CTAs of its row / column from L2.
 constexpr int kStripM = 16;
-__device__ __forceinline__ void tile_coords(int tile, int num_m, int num_n, int& mb, int& nb) {
-    const int strip = tile / (kStripM * num_n);
-    const int r = tile - strip * kStripM * num_n;
-    const int h = min(kStripM, num_m - strip * kStripM);  // the last strip may be shorter
+__device__ __forceinline__ void tile_coords(int tile, int num_m, int num_n, int& mb, int& nb,
+                                            int strip_m = kStripM) {
+    const int strip = tile / (strip_m * num_n);
+    const int r = tile - strip * strip_m * num_n;
+    const int h = min(strip_m, num_m - strip * strip_m);  // the last strip may be shorter
     nb = r / h;
-    mb = strip * kStripM + r % h;
+    mb = strip * strip_m + r % h;
 }
 
+// Clusters of CL CTAs along N: the CL CTAs of a cluster compute the tiles
+// (mb, CL*c + 0 .. CL*c + CL-1) of one cluster tile (mb, c) in lockstep.  They
+// share the A slab of every K block: each CTA loads rows [r*128/CL, (r+1)*128/CL)
+// of it and multicasts them to the whole cluster, so an A panel leaves HBM (or
+// L2) once per cluster instead of once per CTA; B stays per CTA.  Every MMA
+// commit that frees a stage is multicast to the `empty` barriers of all CTAs of
+// the cluster (a CTA may only refill a stage once every peer is done with it).
+template <int CL>
+__device__ __forceinline__ void cluster_tile_coords(int ctile, int num_m, int num_n, int rank, int& mb, int& nb) {
+    tile_coords(ctile, num_m, num_n / CL, mb, nb);
+    nb = nb * CL + rank;
+}
+
+// Epilogue of one output tile (rows mb*128.., columns nb*256..): drains the
+// tile's accumulator groups from TMEM, adds each at its weight into the
+// 128-bit partial sums W and, after the last group, rounds the sums to FP64
+// and writes alpha*r + beta*C.  `release(buf)` hands accumulator `buf` back
+// to the MMA issuer.  Returns false if a wait failed.
+template <class Release>
+__device__ __forceinline__ bool epilogue_tile(const GemmParams& p, int mb, int nb, uint32_t tmem, int quad, int lane,
+                                              ulonglong2* W, uint64_t* accf, uint32_t& acc_it, uint64_t pol_keep,
+                                              uint64_t pol_stream, Release release) {
+    const Schedule& sc = p.sched;
+    const int row = quad * 32 + lane;
+    const int64_t gi = (int64_t)mb * BM + row;
+    const int Ei = p.expA[gi];
+    const int last = sc.n_groups - 1;
+    for (int g = 0; g <= last; ++g, ++acc_it) {
+        const uint32_t buf = acc_it & 1;
+        // all lanes must agree before the warp-collective TMEM loads
+        if (!__all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, p.err, kDevTimeoutAcc)))
+            return false;
+        tc::tc_fence_after();
+        const int sh = sc.gshift[g];
+#pragma unroll 1
+        for (int c = 0; c < BN / 32; ++c) {
+            uint32_t v[32];
+            tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + buf * BN + c * 32, v);
+            // the partial sums of this chunk are requested all at once, and kept
+            // at the back of the L2 eviction order: between two drains of a tile
+            // they must survive the operand tiles streaming through L2
+            ulonglong2 w[32];
+            ulonglong2* wp = W + (c * 32) * BM + row;
+            if (g > 0) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) w[j] = tc::ld_u128_hint(wp + j * BM, pol_keep);
+            }
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int col = c * 32 + j;
+                const int x = __float2int_rn(__uint_as_float(v[j]));
+                unsigned long long lo = 0, hi = 0;
+                if (g > 0) {
+                    lo = w[j].x;
+                    hi = w[j].y;
+                }
+                add_shifted(lo, hi, x, sh);
+                if (g < last) {
+                    tc::st_u128_hint(wp + j * BM, make_ulonglong2(lo, hi), pol_keep);
+                } else {
+                    const int64_t gj = (int64_t)nb * BN + col;
+                    if (gi < p.m && gj < p.n) {
+                        double r = i128_to_double(lo, hi, Ei + p.expB[gj] - p.L);
+                        double* cp = p.C + gi + gj * p.ldc;
+                        // C = fl(fl(alpha*r) + fl(beta*C)), no contraction
+                        if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
+                        if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+                        tc::st_f64_hint(cp, r, pol_stream);
+                    }
+                }
+            }
+        }
+        tc::tc_fence_before();
+        release(buf);
+    }
+    return true;
+}
+
+template <int CL>
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ GemmParams p) {
@@ -377,11 +462,16 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const Schedule& sc = p.sched;
+    const int rank = CL > 1 ? (int)tc::cluster_ctarank() : 0;
+    const int cluster = blockIdx.x / CL, nclusters = gridDim.x / CL;
+    const int num_ctiles = p.num_tiles / CL;
+    constexpr uint16_t kMask = (uint16_t)((1u << CL) - 1);
+    constexpr int A_PART = A_STAGE / CL, A_ROWS = BM / CL;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], CL);  // one commit from every CTA of the cluster
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&accf[b], 1);
@@ -394,6 +484,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
     __syncthreads();
+    // peers multicast into this CTA's shared memory and arrive on its barriers:
+    // every CTA of the cluster must have initialised them first
+    if (CL > 1) tc::cluster_sync();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
@@ -401,37 +494,45 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {  // ---------------------------------- TMA producer
             uint32_t it = 0;
             bool ok = true;
-            for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
+            for (int ct = cluster; ct < num_ctiles && ok; ct += nclusters) {
                 int mb, nb;
-                tile_coords(tile, p.num_m_tiles, p.num_n_tiles, mb, nb);
+                cluster_tile_coords<CL>(ct, p.num_m_tiles, p.num_n_tiles, rank, mb, nb);
                 for (int g = 0; g < sc.n_groups && ok; ++g) {
-                    for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
-                        const int arow = sc.us[u] * sc.a_rows_pad + mb * BM;
-                        const int brow = sc.ut[u] * sc.b_rows_pad + nb * BN;
-                        for (int kb = 0; kb < sc.kb_count; ++kb, ++it) {
-                            const int st = it % STAGES;
-                            if (!tc::mbar_wait(&empty[st], ((it / STAGES) & 1) ^ 1, p.err, kDevTimeoutEmpty)) {
-                                ok = false;
-                                break;
+                    for (int kc = 0; kc < sc.kb_count && ok; kc += KB_CHUNK) {  // same order as the MMA issuer
+                        const int kc1 = min(sc.kb_count, kc + KB_CHUNK);
+                        for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                            const int arow = sc.us[u] * sc.a_rows_pad + mb * BM;
+                            const int brow = sc.ut[u] * sc.b_rows_pad + nb * BN;
+                            for (int kb = kc; kb < kc1; ++kb, ++it) {
+                                const int st = it % STAGES;
+                                if (!tc::mbar_wait(&empty[st], ((it / STAGES) & 1) ^ 1, p.err, kDevTimeoutEmpty)) {
+                                    ok = false;
+                                    break;
+                                }
+                                // this CTA's own bytes plus the A parts its peers multicast in
+                                tc::mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
+                                uint8_t* sa = smem + st * STAGE_BYTES;
+                                if (CL == 1)
+                                    tc::tma_load_2d(sa, &tmA, kb * BK, arow, &full[st]);
+                                else
+                                    tc::tma_load_2d_multicast(sa + rank * A_PART, &tmA, kb * BK, arow + rank * A_ROWS,
+                                                              &full[st], kMask);
+                                tc::tma_load_2d(sa + A_STAGE, &tmB, kb * BK, brow, &full[st]);
                             }
-                            tc::mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
-                            uint8_t* sa = smem + st * STAGE_BYTES;
-                            tc::tma_load_2d(sa, &tmA, kb * BK, arow, &full[st]);
-                            tc::tma_load_2d(sa + A_STAGE, &tmB, kb * BK, brow, &full[st]);
                         }
                     }
                 }
             }
             // let the copies in flight land before the CTA can exit
             const uint32_t first = it > STAGES ? it - STAGES : 0;
-            for (uint32_t j = first; j < it; ++j) tc::mbar_wait(&full[j % STAGES], (j / STAGES) & 1, p.err, 0);
+            for (uint32_t j = first; j < it; ++j) tc::mbar_wait_drain(&full[j % STAGES], (j / STAGES) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---------------------------------- MMA issuer
             constexpr uint32_t ID = tc::idesc(tc::kFmtE4M3, tc::kFmtE4M3, BM, BN);
             uint32_t it = 0, acc_it = 0;
             bool ok = true;
-            for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
+            for (int ct = cluster; ct < num_ctiles && ok; ct += nclusters) {
                 for (int g = 0; g < sc.n_groups && ok; ++g, ++acc_it) {
                     const uint32_t buf = acc_it & 1;
                     if (!tc::mbar_wait(&acce[buf], ((acc_it >> 1) & 1) ^ 1, p.err, kDevTimeoutAccEmpty)) {
@@ -441,22 +542,30 @@ __global__ void __launch_bounds__(THREADS, 1)
                     tc::tc_fence_after();
                     const uint32_t d_tmem = tmem + buf * BN;
                     uint32_t accumulate = 0;
-                    for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
-                        for (int kb = 0; kb < sc.kb_count; ++kb, ++it) {
-                            const int st = it % STAGES;
-                            if (!tc::mbar_wait(&full[st], (it / STAGES) & 1, p.err, kDevTimeoutFull)) {
-                                ok = false;
-                                break;
-                            }
-                            tc::tc_fence_after();
-                            const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES);
-                            const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + A_STAGE);
+                    // K-chunk-major within the group: every slice product of the group
+                    // advances through one 512-wide K chunk before the next chunk, so a
+                    // wave of CTAs shares a small, L2-resident set of operand panels
+                    // (the integer sum in the accumulator does not depend on the order)
+                    for (int kc = 0; kc < sc.kb_count && ok; kc += KB_CHUNK) {
+                        const int kc1 = min(sc.kb_count, kc + KB_CHUNK);
+                        for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                            for (int kb = kc; kb < kc1; ++kb, ++it) {
+                                const int st = it % STAGES;
+                                if (!tc::mbar_wait(&full[st], (it / STAGES) & 1, p.err, kDevTimeoutFull)) {
+                                    ok = false;
+                                    break;
+                                }
+                                tc::tc_fence_after();
+                                const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES);
+                                const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + A_STAGE);
 #pragma unroll
-                            for (int kk = 0; kk < BK / 32; ++kk) {
-                                tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
-                                accumulate = 1;
+                                for (int kk = 0; kk < BK / 32; ++kk) {
+                                    tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
+                                    accumulate = 1;
+                                }
+                                if (CL == 1) tc::mma_commit(&empty[st]);
+                                else tc::mma_commit_multicast(&empty[st], kMask);
                             }
-                            tc::mma_commit(&empty[st]);
                         }
                     }
                     if (ok) tc::mma_commit(&accf[buf]);
@@ -464,77 +573,198 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             // every MMA must be complete before TMEM is released
             tc::mma_commit(drain);
-            tc::mbar_wait(drain, 0, p.err, 0);
+            tc::mbar_wait_drain(drain, 0);
         }
     } else {  // ------------------------------------------------ epilogue
         const int quad = warp & 3;  // TMEM lanes this warp may access
-        const int row = quad * 32 + lane;
         ulonglong2* W = p.W + (size_t)blockIdx.x * (BM * BN);
         const uint64_t pol_keep = tc::policy_evict_last(), pol_stream = tc::policy_evict_first();
         uint32_t acc_it = 0;
-        bool ok = true;
-        const int last = sc.n_groups - 1;
-        for (int tile = blockIdx.x; tile < p.num_tiles && ok; tile += gridDim.x) {
+        for (int ct = cluster; ct < num_ctiles; ct += nclusters) {
             int mb, nb;
-            tile_coords(tile, p.num_m_tiles, p.num_n_tiles, mb, nb);
-            const int64_t gi = (int64_t)mb * BM + row;
-            const int Ei = p.expA[gi];
-            for (int g = 0; g <= last && ok; ++g, ++acc_it) {
-                const uint32_t buf = acc_it & 1;
-                // all lanes must agree before the warp-collective TMEM loads
-                ok = __all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, p.err, kDevTimeoutAcc));
-                if (!ok) break;
-                tc::tc_fence_after();
-                const int sh = sc.gshift[g];
-#pragma unroll 1
-                for (int c = 0; c < BN / 32; ++c) {
-                    uint32_t v[32];
-                    tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + buf * BN + c * 32, v);
-                    // the partial sums of this chunk are requested all at once, and kept
-                    // at the back of the L2 eviction order: between two drains of a tile
-                    // they must survive the operand tiles streaming through L2
-                    ulonglong2 w[32];
-                    ulonglong2* wp = W + (c * 32) * BM + row;
-                    if (g > 0) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) w[j] = tc::ld_u128_hint(wp + j * BM, pol_keep);
-                    }
-                    tc::tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int col = c * 32 + j;
-                        const int x = __float2int_rn(__uint_as_float(v[j]));
-                        unsigned long long lo = 0, hi = 0;
-                        if (g > 0) {
-                            lo = w[j].x;
-                            hi = w[j].y;
-                        }
-                        add_shifted(lo, hi, x, sh);
-                        if (g < last) {
-                            tc::st_u128_hint(wp + j * BM, make_ulonglong2(lo, hi), pol_keep);
-                        } else {
-                            const int64_t gj = (int64_t)nb * BN + col;
-                            if (gi < p.m && gj < p.n) {
-                                double r = i128_to_double(lo, hi, Ei + p.expB[gj] - p.L);
-                                double* cp = p.C + gi + gj * p.ldc;
-                                // C = fl(fl(alpha*r) + fl(beta*C)), no contraction
-                                if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
-                                if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
-                                tc::st_f64_hint(cp, r, pol_stream);
-                            }
-                        }
-                    }
-                }
-                tc::tc_fence_before();
-                tc::mbar_arrive(&acce[buf]);
-            }
+            cluster_tile_coords<CL>(ct, p.num_m_tiles, p.num_n_tiles, rank, mb, nb);
+            if (!epilogue_tile(p, mb, nb, tmem, quad, lane, W, accf, acc_it, pol_keep, pol_stream,
+                               [&](uint32_t buf) { tc::mbar_arrive(&acce[buf]); }))
+                break;
         }
     }
     __syncthreads();
+    // no CTA leaves while a peer may still multicast into it or arrive on it
+    if (CL > 1) tc::cluster_sync();
     if (warp == 1) {
         __syncwarp();
         tc::tc_fence_after();
         tc::tmem_dealloc(tmem, 512);
+    }
+}
+
+// CTA-pair form of the slice-product GEMM, used when m spans two or more
+// 128-row tiles.  A cluster of 2 CTAs computes one 256 x 256 output tile with
+// tcgen05.mma.cta_group::2 (M = 256 over the pair).  Per K block each CTA
+// loads its own 128 rows of the A slab and one half (128 rows) of the B slab:
+// 32 KB per stage and SM instead of 48 KB, so operand traffic from L2 falls by
+// a third for the same MMA work.  The even CTA issues the MMAs and owns the
+// `full` barriers, on which the TMA loads of both CTAs count; its MMA commits
+// free the stages and the accumulators of both CTAs.  Each CTA drains the
+// accumulator of its own 128 rows, and both epilogues hand an accumulator
+// back on the even CTA's `acce` barrier.
+//
+// Four stages, not the seven that would fit: the operands of a wave of tiles
+// are shared through L2 only while the CTAs of the wave stay close together
+// in their K stream.  A deeper ring lets each CTA run further ahead, spreads
+// the wave's working set past the L2 and multiplies HBM traffic; measured at
+// m = n = k = 16384, 4 stages took 275 ms, 5 took 323 ms and 7 took 427 ms
+// (DRAM reads 2.9 TB at 7 stages).
+constexpr int P_STAGES = 4;
+constexpr int P_A = BM * BK, P_B = (BN / 2) * BK, P_STAGE = P_A + P_B;
+constexpr int P_SMEM_BYTES = P_STAGES * P_STAGE + 1024 + 256;
+static_assert(P_SMEM_BYTES <= 232448, "pair GEMM shared memory");
+
+__global__ void __launch_bounds__(THREADS, 1)
+    ozaki_gemm_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                           const __grid_constant__ GemmParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + P_STAGES * P_STAGE);
+    uint64_t* empty = full + P_STAGES;
+    uint64_t* accf = empty + P_STAGES;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Schedule& sc = p.sched;
+    const int rank = (int)tc::cluster_ctarank();
+    const bool leader = rank == 0;
+    const int pair = blockIdx.x / 2, npairs = gridDim.x / 2;
+    const int num_pm = p.num_m_tiles / 2;  // 256-row tiles
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P_STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);   // the even CTA's expect_tx (bytes of both CTAs)
+            tc::mbar_init(&empty[s], 1);  // one MMA commit per use
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&accf[b], 1);
+            tc::mbar_init(&acce[b], 8);  // the 4 epilogue warps of each CTA
+        }
+        tc::mbar_init(drain, 1);
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) tc::tmem_alloc_pair(tmem_slot, 512);
+    __syncthreads();
+    // the peer's loads and commits reach this CTA's barriers: both CTAs must
+    // have initialised them first
+    tc::cluster_sync();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---------------------------------- TMA producer (both CTAs)
+            const uint32_t full0 = tc::mapa_shared(full, 0);  // full[0] of the even CTA
+            uint32_t it = 0;
+            bool ok = true;
+            for (int ct = pair; ct < p.num_tiles && ok; ct += npairs) {
+                int mbp, nb;
+                tile_coords(ct, num_pm, p.num_n_tiles, mbp, nb, kStripM / 2);
+                const int mb = 2 * mbp + rank;
+                for (int g = 0; g < sc.n_groups && ok; ++g) {
+                    for (int kc = 0; kc < sc.kb_count && ok; kc += KB_CHUNK) {  // same order as the MMA issuer
+                        const int kc1 = min(sc.kb_count, kc + KB_CHUNK);
+                        for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                            const int arow = sc.us[u] * sc.a_rows_pad + mb * BM;
+                            const int brow = sc.ut[u] * sc.b_rows_pad + nb * BN + rank * (BN / 2);
+                            for (int kb = kc; kb < kc1; ++kb, ++it) {
+                                const int st = it % P_STAGES;
+                                if (!tc::mbar_wait(&empty[st], ((it / P_STAGES) & 1) ^ 1, p.err, kDevTimeoutEmpty)) {
+                                    ok = false;
+                                    break;
+                                }
+                                if (leader) tc::mbar_arrive_expect_tx(&full[st], 2 * P_STAGE);
+                                uint8_t* sa = smem + st * P_STAGE;
+                                tc::tma_load_2d_pair(sa, &tmA, kb * BK, arow, full0 + st * 8);
+                                tc::tma_load_2d_pair(sa + P_A, &tmB, kb * BK, brow, full0 + st * 8);
+                            }
+                        }
+                    }
+                }
+            }
+            // the even CTA's last stages count the copies of both CTAs: once they
+            // are complete nothing is in flight into either CTA
+            if (leader) {
+                const uint32_t first = it > P_STAGES ? it - P_STAGES : 0;
+                for (uint32_t j = first; j < it; ++j) tc::mbar_wait_drain(&full[j % P_STAGES], (j / P_STAGES) & 1);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && leader) {  // ------------------------ MMA issuer (even CTA)
+            constexpr uint32_t ID = tc::idesc(tc::kFmtE4M3, tc::kFmtE4M3, 2 * BM, BN);
+            uint32_t it = 0, acc_it = 0;
+            bool ok = true;
+            for (int ct = pair; ct < p.num_tiles && ok; ct += npairs) {
+                for (int g = 0; g < sc.n_groups && ok; ++g, ++acc_it) {
+                    const uint32_t buf = acc_it & 1;
+                    if (!tc::mbar_wait_cluster(&acce[buf], ((acc_it >> 1) & 1) ^ 1, p.err, kDevTimeoutAccEmpty)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t d_tmem = tmem + buf * BN;
+                    uint32_t accumulate = 0;
+                    for (int kc = 0; kc < sc.kb_count && ok; kc += KB_CHUNK) {
+                        const int kc1 = min(sc.kb_count, kc + KB_CHUNK);
+                        for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                            for (int kb = kc; kb < kc1; ++kb, ++it) {
+                                const int st = it % P_STAGES;
+                                if (!tc::mbar_wait(&full[st], (it / P_STAGES) & 1, p.err, kDevTimeoutFull)) {
+                                    ok = false;
+                                    break;
+                                }
+                                tc::tc_fence_after();
+                                const uint32_t sa = tc::smem_u32(smem + st * P_STAGE);
+                                const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + P_A);
+#pragma unroll
+                                for (int kk = 0; kk < BK / 32; ++kk) {
+                                    tc::mma_pair_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
+                                    accumulate = 1;
+                                }
+                                tc::mma_pair_commit_multicast(&empty[st], 3);
+                            }
+                        }
+                    }
+                    if (ok) tc::mma_pair_commit_multicast(&accf[buf], 3);
+                }
+            }
+            // every MMA must be complete before either CTA releases its TMEM
+            tc::mma_pair_commit_multicast(drain, 1);
+            tc::mbar_wait_drain(drain, 0);
+        }
+    } else {  // ------------------------------------------------ epilogue (both CTAs)
+        const int quad = warp & 3;
+        ulonglong2* W = p.W + (size_t)blockIdx.x * (BM * BN);
+        const uint64_t pol_keep = tc::policy_evict_last(), pol_stream = tc::policy_evict_first();
+        const uint32_t acce0 = tc::mapa_shared(acce, 0);
+        uint32_t acc_it = 0;
+        for (int ct = pair; ct < p.num_tiles; ct += npairs) {
+            int mbp, nb;
+            tile_coords(ct, num_pm, p.num_n_tiles, mbp, nb, kStripM / 2);
+            if (!epilogue_tile(p, 2 * mbp + rank, nb, tmem, quad, lane, W, accf, acc_it, pol_keep, pol_stream,
+                               [&](uint32_t buf) {
+                                   __syncwarp();
+                                   if (lane == 0) tc::mbar_arrive_cluster(acce0 + buf * 8);
+                               }))
+                break;
+        }
+    }
+    __syncthreads();
+    // the even CTA's MMAs read this CTA's shared memory and write its TMEM
+    tc::cluster_sync();
+    if (warp == 1) {
+        __syncwarp();
+        tc::tc_fence_after();
+        tc::tmem_dealloc_pair(tmem, 512);
     }
 }
 
@@ -664,6 +894,128 @@ int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t 
     return COSMA_GPU_SUCCESS;
 }
 
+// Which form of the slice-product GEMM runs, and the padded operand extents
+// it needs.  The CTA-pair form (256 x 256 tiles) runs whenever m spans two or
+// more 128-row tiles and padding m to 256 costs at most ~10% more work; the
+// single-CTA form (128 x 256 tiles) takes the rest, in clusters of CL CTAs
+// along N that share the A slab by multicast: the widest of 4, 2, 1 whose
+// padding of the N tiles costs at most ~10% more work.
+struct GemmShape {
+    bool pair;
+    int cl;  // cluster width of the single-CTA form (2 for the pair form)
+    int64_t m_pad, n_pad;
+};
+
+GemmShape gemm_shape(int64_t m, int64_t n) {
+    GemmShape g;
+    const int64_t mt = ceil_div(m, BM), nt = ceil_div(n, BN);
+    g.pair = mt >= 2 && (mt % 2 == 0 || mt >= 10);
+    if (g.pair) {
+        g.cl = 2;
+        g.m_pad = ceil_div(m, 2 * BM) * 2 * BM;
+        g.n_pad = nt * BN;
+        return g;
+    }
+    g.cl = 1;
+    for (int cl : {4, 2}) {
+        if (nt >= cl && ceil_div(nt, cl) * cl * 10 <= nt * 11) {
+            g.cl = cl;
+            break;
+        }
+    }
+    g.m_pad = mt * BM;
+    g.n_pad = ceil_div(nt, g.cl) * g.cl * BN;
+    return g;
+}
+
+template <class Kernel>
+int max_active_clusters(Kernel kern, int cl, int smem, int* out) {
+    CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl * num_sms(), 1, 1);
+    cfg.blockDim = dim3(THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = cl;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    CGB_CUDA(cudaOccupancyMaxActiveClusters(out, kern, &cfg));
+    return COSMA_GPU_SUCCESS;
+}
+
+// Persistent grid: as many whole clusters as fit on the GPU at once (one CTA
+// per SM), but no more than there are cluster tiles.  num_tiles counts CTA
+// tiles for the single-CTA form and 256 x 256 tiles for the pair form.
+int gemm_grid(const GemmShape& sh, int num_tiles, int* grid) {
+    static int max_clusters[6] = {0, 0, 0, 0, 0, 0};  // [cl] single-CTA form, [5] pair form
+    const int slot = sh.pair ? 5 : sh.cl;
+    if (!max_clusters[slot]) {
+        int n = 0;
+        if (sh.pair) CGB_CHECK(max_active_clusters(ozaki_gemm_pair_kernel, 2, P_SMEM_BYTES, &n));
+        else if (sh.cl == 1) n = num_sms();
+        else if (sh.cl == 2) CGB_CHECK(max_active_clusters(ozaki_gemm_kernel<2>, 2, SMEM_BYTES, &n));
+        else CGB_CHECK(max_active_clusters(ozaki_gemm_kernel<4>, 4, SMEM_BYTES, &n));
+        n = std::min(n, num_sms() / sh.cl);  // one CTA per SM: never more CTAs than SMs
+        if (n < 1) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki: no cluster of the slice GEMM fits on the GPU");
+        max_clusters[slot] = n;
+    }
+    const int cluster_tiles = sh.pair ? num_tiles : num_tiles / sh.cl;
+    *grid = std::min(cluster_tiles, max_clusters[slot]) * sh.cl;
+    return COSMA_GPU_SUCCESS;
+}
+
+// Fills the tile counts of p for the chosen form.
+void set_tiles(const GemmShape& sh, GemmParams& p) {
+    p.num_m_tiles = (int)(sh.m_pad / BM);
+    p.num_n_tiles = (int)(sh.n_pad / BN);
+    p.num_tiles = sh.pair ? (p.num_m_tiles / 2) * p.num_n_tiles : p.num_m_tiles * p.num_n_tiles;
+}
+
+template <class Kernel>
+int launch_cluster(Kernel kern, int cl, int grid, int smem, const CUtensorMap& tmA, const CUtensorMap& tmB,
+                   const GemmParams& p, cudaStream_t st) {
+    CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid, 1, 1);
+    cfg.blockDim = dim3(THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = cl;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    CGB_CUDA(cudaLaunchKernelEx(&cfg, kern, tmA, tmB, p));
+    return COSMA_GPU_SUCCESS;
+}
+
+// Launches the slice-product GEMM over digit slices laid out [S][rows_pad][k_pad].
+int launch_slice_gemm(const GemmShape& sh, int grid, const void* slicesA, const void* slicesB, int S, int64_t k_pad,
+                      const GemmParams& p, cudaStream_t st) {
+    CUtensorMap tmA, tmB;
+    // single-CTA clusters: each CTA loads BM/cl rows of the A slab and
+    // multicasts them; pairs: each CTA loads its 128 rows of A and half of B
+    const int a_box = sh.pair ? BM : BM / sh.cl, b_box = sh.pair ? BN / 2 : BN;
+    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slicesA, (uint64_t)k_pad,
+                           (uint64_t)(S * sh.m_pad), (uint64_t)k_pad, BK, a_box));
+    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slicesB, (uint64_t)k_pad,
+                           (uint64_t)(S * sh.n_pad), (uint64_t)k_pad, BK, b_box));
+    if (sh.pair) return launch_cluster(ozaki_gemm_pair_kernel, 2, grid, P_SMEM_BYTES, tmA, tmB, p, st);
+    if (sh.cl == 1) {
+        CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        ozaki_gemm_kernel<1><<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
+        CGB_CUDA(cudaGetLastError());
+        return COSMA_GPU_SUCCESS;
+    }
+    if (sh.cl == 2) return launch_cluster(ozaki_gemm_kernel<2>, 2, grid, SMEM_BYTES, tmA, tmB, p, st);
+    return launch_cluster(ozaki_gemm_kernel<4>, 4, grid, SMEM_BYTES, tmA, tmB, p, st);
+}
+
 // One call with k <= MAX_K_PER_CALL.
 int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_info* info) {
     const int64_t m = g.m, n = g.n, k = g.k;
@@ -672,7 +1024,8 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
     const double* B = (const double*)g.B;
     Workspace* w = workspace(st);
     if (!w->host_stats || !w->host_err) return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "ozaki: pinned staging");
-    const int64_t m_pad = ceil_div(m, BM) * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BK) * BK;
+    const GemmShape shape = gemm_shape(m, n);
+    const int64_t m_pad = shape.m_pad, n_pad = shape.n_pad, k_pad = ceil_div(k, BK) * BK;
 
     // 1. scaling + spread statistics
     CGB_CHECK(w->stats.reserve(sizeof(Stats), st));
@@ -714,9 +1067,7 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
     std::memset(&p, 0, sizeof(p));
     int L = 0;
     CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &L));
-    p.num_m_tiles = (int)(m_pad / BM);
-    p.num_n_tiles = (int)(n_pad / BN);
-    p.num_tiles = (int)((m_pad / BM) * (n_pad / BN));
+    set_tiles(shape, p);
     p.m = m; p.n = n; p.ldc = g.ldc;
     p.C = (double*)g.C;
     p.expA = (const int*)w->expA.ptr;
@@ -726,23 +1077,13 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
     p.beta_zero = g.beta[0] == 0.0;
     p.alpha_one = g.alpha[0] == 1.0;
     p.L = L;
-    const int grid = std::min(p.num_tiles, num_sms());
+    int grid = 0;
+    CGB_CHECK(gemm_grid(shape, p.num_tiles, &grid));
     CGB_CHECK(w->W.reserve((size_t)grid * BM * BN * sizeof(ulonglong2), st));
     p.W = (ulonglong2*)w->W.ptr;
     p.err = (unsigned*)w->err.ptr;
-    CUtensorMap tmA, tmB;
-    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, w->slicesA.ptr, (uint64_t)k_pad,
-                           (uint64_t)(S * m_pad), (uint64_t)k_pad, BK, BM));
-    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, w->slicesB.ptr, (uint64_t)k_pad,
-                           (uint64_t)(S * n_pad), (uint64_t)k_pad, BK, BN));
-    static bool attr = false;
-    if (!attr) {
-        CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        attr = true;
-    }
     CGB_CUDA(cudaEventRecord(w->ev[2], st));
-    ozaki_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
-    CGB_CUDA(cudaGetLastError());
+    CGB_CHECK(launch_slice_gemm(shape, grid, w->slicesA.ptr, w->slicesB.ptr, S, k_pad, p, st));
     CGB_CUDA(cudaEventRecord(w->ev[3], st));
     CGB_CUDA(cudaMemcpyAsync(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CGB_CUDA(cudaStreamSynchronize(st));
@@ -848,7 +1189,8 @@ struct NoAllocLayout {
 };
 
 NoAllocLayout noalloc_layout(int64_t m, int64_t n, int64_t k, int S, bool a_kcontig, bool b_kcontig) {
-    const int64_t m_pad = ceil_div(m, BM) * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BK) * BK;
+    const GemmShape shape = gemm_shape(m, n);
+    const int64_t m_pad = shape.m_pad, n_pad = shape.n_pad, k_pad = ceil_div(k, BK) * BK;
     NoAllocLayout L;
     size_t off = 0;
     L.stats = off; off += align256(sizeof(Stats));
@@ -881,7 +1223,8 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
     const bool ta = g.opa != 0, tb = g.opb != 0;
     const double* A = (const double*)g.A;
     const double* B = (const double*)g.B;
-    const int64_t m_pad = ceil_div(m, BM) * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BK) * BK;
+    const GemmShape shape = gemm_shape(m, n);
+    const int64_t m_pad = shape.m_pad, n_pad = shape.n_pad, k_pad = ceil_div(k, BK) * BK;
     // Reject before touching the device: the smallest slice count must fit.
     const NoAllocLayout L2 = noalloc_layout(m, n, k, slices > 0 ? std::min(slices, MAX_SLICES) : 2, ta, !tb);
     if (L2.total > kNoAllocScratchBytes) return too_large(L2.total);
@@ -946,9 +1289,7 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
     std::memset(&p, 0, sizeof(p));
     int Lw = 0;
     CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &Lw));
-    p.num_m_tiles = (int)(m_pad / BM);
-    p.num_n_tiles = (int)(n_pad / BN);
-    p.num_tiles = (int)((m_pad / BM) * (n_pad / BN));
+    set_tiles(shape, p);
     p.m = m; p.n = n; p.ldc = g.ldc;
     p.C = (double*)g.C;
     p.expA = expA;
@@ -960,15 +1301,9 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
     p.L = Lw;
     p.W = (ulonglong2*)(sc + L.W);
     p.err = err_dev;
-    const int grid = std::min(p.num_tiles, num_sms());
-    CUtensorMap tmA, tmB;
-    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slA, (uint64_t)k_pad, (uint64_t)(S * m_pad),
-                           (uint64_t)k_pad, BK, BM));
-    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slB, (uint64_t)k_pad, (uint64_t)(S * n_pad),
-                           (uint64_t)k_pad, BK, BN));
-    CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    ozaki_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
-    CGB_CUDA(cudaGetLastError());
+    int grid = 0;
+    CGB_CHECK(gemm_grid(shape, p.num_tiles, &grid));  // <= num_sms(), the CTAs W was sized for
+    CGB_CHECK(launch_slice_gemm(shape, grid, slA, slB, S, k_pad, p, st));
     unsigned herr = 0;
     CGB_CUDA(cudaMemcpyAsync(&herr, err_dev, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CGB_CUDA(cudaStreamSynchronize(st));

@@ -94,6 +94,38 @@ def ozaki_gemm(ta, tb, A, B, S):
     return C
 
 
+def ozaki_gemm_sampled(ta, tb, A, B, S, rows, cols):
+    """The same exact result at the sampled entries (rows[i], cols[i]) only.
+
+    Row and column exponents depend on one row of op(A) / one column of
+    op(B) each, so restricting to the sampled rows and columns is exact; this
+    pins large problems (many tiles per CTA) at a cost linear in the sample.
+    """
+    opA = np.asarray(A if ta in "Nn" else A.T, dtype=np.float64)
+    opB = np.asarray(B if tb in "Nn" else B.T, dtype=np.float64)
+    rows = np.asarray(rows, dtype=np.int64)
+    cols = np.asarray(cols, dtype=np.int64)
+    Ar = opA[rows]                     # samples x k
+    Bc = opB[:, cols].T                # samples x k
+    EA = row_exponents(opA)[rows]
+    EB = row_exponents(opB.T)[cols]
+    DA = digits(Ar, EA[:, None], S)    # samples x k x S
+    DB = digits(Bc, EB[:, None], S)
+    L = 8 + 5 * (S - 1)
+    out = np.zeros(len(rows))
+    V = [0] * len(rows)
+    for s in range(1, S + 1):
+        for t in range(1, S + 2 - s):
+            P = np.einsum("ik,ik->i", DA[:, :, s - 1], DB[:, :, t - 1])  # exact in int64
+            w = 1 << (5 * (S + 1 - s - t))
+            for i in range(len(rows)):
+                V[i] += int(P[i]) * w
+    for i in range(len(rows)):
+        e = int(EA[i] + EB[i] - L)
+        out[i] = float(Fraction(V[i]) * (Fraction(2) ** e))
+    return out
+
+
 def error_bound_bits(S):
     """Fraction bits F = 4 + 5(S-1) carried by S slices."""
     return 4 + 5 * (S - 1)

@@ -46,6 +46,27 @@ def test_bit_exact_against_restatement(native_lib, cuda, ta, tb, m, n, k, S):
     np.testing.assert_array_equal(got, ref)
 
 
+# Both forms of the slice-product GEMM, at sizes with several tiles per CTA
+# (persistent loop, partial sums reused across tiles), checked bit for bit on
+# sampled entries, edges included.
+@pytest.mark.parametrize("ta,tb,m,n,k,S", [
+    ("N", "N", 2560, 2304, 256, 5),   # CTA pairs, 90 tiles of 256 x 256
+    ("T", "N", 1300, 700, 300, 13),   # CTA pairs, m padded to 1536
+    ("N", "T", 1152, 5120, 200, 6),   # single CTAs in clusters of 4 along N, 180 tiles
+    ("T", "T", 384, 512, 130, 9),     # single CTAs in clusters of 2
+    ("N", "N", 640, 1280, 70, 7),     # single CTAs, no cluster
+])
+def test_bit_exact_sampled_gemm_forms(native_lib, cuda, ta, tb, m, n, k, S):
+    A = oracle.exp_spread(_op_shape(ta, m, k), m + 3, 6)
+    B = oracle.exp_spread(_op_shape(tb, k, n), n + 5, 6)
+    got, info = _run(ta, tb, m, n, k, A, B, slices=S)
+    rng = np.random.default_rng(m + n)
+    rows = np.concatenate([rng.integers(0, m, 1500), [0, m - 1, m - 1, 0]])
+    cols = np.concatenate([rng.integers(0, n, 1500), [0, n - 1, 0, n - 1]])
+    ref = oz.ozaki_gemm_sampled(ta, tb, A, B, S, rows, cols)
+    np.testing.assert_array_equal(got[rows, cols], ref)
+
+
 def test_fp32_accumulation_is_exact_at_k16384(native_lib, cuda):
     rng = np.random.default_rng(1)
     m, n, k = 256, 256, 16384

@@ -73,3 +73,15 @@ def test_integer_inputs_are_exact():
     B = np.asfortranarray(rng.integers(-15, 16, (40, 5)).astype(np.float64))
     C = ozaki.ozaki_gemm("N", "N", A, B, 3)
     np.testing.assert_array_equal(C, A @ B)
+
+
+def test_sampled_restatement_matches_full():
+    rng = np.random.default_rng(3)
+    for ta, tb in (("N", "N"), ("T", "N"), ("N", "T")):
+        m, n, k, S = 23, 17, 41, 6
+        A = oracle.exp_spread((m, k) if ta == "N" else (k, m), 4, 5)
+        B = oracle.exp_spread((k, n) if tb == "N" else (n, k), 5, 5)
+        full = ozaki.ozaki_gemm(ta, tb, A, B, S)
+        rows = rng.integers(0, m, 60)
+        cols = rng.integers(0, n, 60)
+        np.testing.assert_array_equal(ozaki.ozaki_gemm_sampled(ta, tb, A, B, S, rows, cols), full[rows, cols])
