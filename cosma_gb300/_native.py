@@ -73,6 +73,8 @@ SIGNATURES = {
     "cosma_gpu_cgemm_device": (i32, [i32, ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "cosma_gpu_dgemm_ozaki_device": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                            C.POINTER(OzakiInfo)]),
+    "cosma_gpu_zgemm_ozaki_device": (i32, [ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, i32, vp,
+                                           C.POINTER(OzakiInfo)]),
     "cosma_gpu_dgemm_ozaki_noalloc": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                             C.POINTER(OzakiInfo)]),
     "cosma_gpu_grouped_plan_create": (vp, [i32, i32, C.POINTER(GemmProblem), i32, vp]),

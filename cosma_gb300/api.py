@@ -203,6 +203,17 @@ def dgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm,
     return info.as_dict()
 
 
+def zgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc, slices=0, stream=None):
+    """FP64-accurate Ozaki-split ZGEMM (complex128 CUDA buffers, op N/T/C);
+    returns the slice statistics."""
+    lib = N.load()
+    info = N.OzakiInfo()
+    al, be = _cplx_pair(alpha, C.c_double), _cplx_pair(beta, C.c_double)
+    N.check(lib.cosma_gpu_zgemm_ozaki_device(transa.encode(), transb.encode(), m, n, k, al, ptr(A), lda, ptr(B),
+                                             ldb, be, ptr(Cm), ldc, slices, _stream_ptr(stream), C.byref(info)))
+    return info.as_dict()
+
+
 class GroupedPlan:
     """A grouped FP64 GEMM over many device problems, one persistent launch
     replayed from a CUDA graph.  `problems` is a list of tuples

@@ -45,7 +45,9 @@ int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t st
         method = g.scalar == Scalar::S ? COSMA_GPU_METHOD_BF16X3 : COSMA_GPU_METHOD_NATIVE;
     if (method == COSMA_GPU_METHOD_OZAKI) {
         if (g.scalar == Scalar::D) return ozaki_dgemm(g, ozaki_slices, stream, info);
-        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "gemm: the Ozaki method is implemented for double");
+        if (g.scalar == Scalar::Z) return ozaki_zgemm(g, ozaki_slices, stream, info);
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED,
+                         "gemm: the Ozaki method is implemented for double and complex double");
     }
     if (method == COSMA_GPU_METHOD_BF16X3) {
         if (g.scalar == Scalar::S) return bf16x3_sgemm(g, stream);
@@ -120,6 +122,14 @@ int cosma_gpu_dgemm_ozaki_device(char ta, char tb, int64_t m, int64_t n, int64_t
     cgb::clear_error();
     double a[2] = {alpha, 0}, b[2] = {beta, 0};
     auto g = cgb::make_desc(cgb::Scalar::D, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc);
+    return cgb::gemm_device(g, COSMA_GPU_METHOD_OZAKI, slices, (cudaStream_t)stream, info);
+}
+
+int cosma_gpu_zgemm_ozaki_device(char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,
+                                 const double* A, int64_t lda, const double* B, int64_t ldb, const double* beta,
+                                 double* C, int64_t ldc, int slices, void* stream, cosma_gpu_ozaki_info* info) {
+    cgb::clear_error();
+    auto g = cgb::make_desc(cgb::Scalar::Z, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     return cgb::gemm_device(g, COSMA_GPU_METHOD_OZAKI, slices, (cudaStream_t)stream, info);
 }
 

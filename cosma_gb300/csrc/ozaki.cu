@@ -80,6 +80,11 @@ struct Schedule {
 struct GemmParams {
     int num_m_tiles, num_n_tiles, num_tiles;
     int64_t m, n, ldc;
+    // complex results: GEMM columns [0, n_split) are the real parts of C's
+    // columns, [n_split, 2*n_split) the imaginary parts; cs = 2 doubles per
+    // element.  Real results: n_split beyond every column, cs = 1.
+    int64_t n_split;
+    int cs;
     double* C;
     const int* expA;
     const int* expB;
@@ -179,17 +184,21 @@ __global__ void scale_kcontig_kernel(const double* __restrict__ X, int64_t ld, i
 
 // Rows contiguous in memory (op(A) stored as is, op(B) stored transposed):
 // one thread per row over a chunk of K; partial states combined afterwards.
-__global__ void scale_mcontig_partial_kernel(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t k,
-                                             int64_t kchunk, int* __restrict__ pe, float* __restrict__ pm,
-                                             Stats* st) {
+// es = 2 for complex data viewed as doubles: element (row, l) is the pair
+// X[2*row + l*ld], X[2*row + 1 + l*ld] and both parts count.
+__global__ void scale_mcontig_partial_kernel(const double* __restrict__ X, int64_t ld, int es, int64_t rows,
+                                             int64_t k, int64_t kchunk, int* __restrict__ pe,
+                                             float* __restrict__ pm, Stats* st) {
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     const int64_t l0 = (int64_t)blockIdx.y * kchunk, l1 = min(k, l0 + kchunk);
     RowState s{-(1 << 30), 0.0f};
     unsigned bad = 0;
     for (int64_t l = l0; l < l1; ++l) {
-        int lb;
-        if (element_log2(X[row + l * ld], &lb, &bad)) state_add(s, lb);
+        for (int c = 0; c < es; ++c) {
+            int lb;
+            if (element_log2(X[row * es + c + l * ld], &lb, &bad)) state_add(s, lb);
+        }
     }
     if (bad) atomicOr(&st->nonfinite, 1u);
     pe[blockIdx.y * rows + row] = s.emax;
@@ -281,6 +290,70 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
     for (int s = 0; s < S; ++s) {
         uint4 v = make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
         *reinterpret_cast<uint4*>(out + (int64_t)s * rows_pad * k_pad + r * k_pad + l0) = v;
+    }
+}
+
+// Complex operands.  One real GEMM of depth 2*kh gives both parts of C:
+//   A_cat row r                 [ Re a | sa*Im a ]
+//   B_cat row r                 [ Re b | -sb*Im b ]   -> Re C column r
+//   B_cat row half_rows + r     [ sb*Im b | Re b ]    -> Im C column r
+// (sa, sb = -1 for a conjugated operand), so that
+//   Re c = sum Re a Re b - Im a Im b,  Im c = sum Re a Im b + Im a Re b
+// accumulate exactly in the same 128-bit integers as the real case.  Both
+// parts of a row share its exponent.  Digits of -x are the negated digits of
+// x, so a negation flips the sign bit of every E4M3 byte (zero becomes -0,
+// which the MMA adds as 0).  kh is k padded to 64; the row pitch is 2*kh;
+// slice s starts at s * slice_rows * 2*kh.  X holds interleaved complex
+// doubles, ld in complex elements.
+template <int S, bool KCONTIG, bool BSIDE>
+__global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restrict__ X, int64_t ld, int64_t rows,
+                                                         int64_t k, const int* __restrict__ exps, int64_t kh,
+                                                         int64_t rows_pad, int64_t slice_rows, uint32_t conj_mask,
+                                                         uint8_t* __restrict__ out) {
+    const int t = threadIdx.x;
+    int64_t r;
+    int kc;
+    if (KCONTIG) { r = (int64_t)blockIdx.x * 64 + t / 4; kc = t % 4; }
+    else { r = (int64_t)blockIdx.x * 64 + t % 64; kc = t / 64; }
+    const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 16;
+    if (r >= rows_pad || l0 >= kh) return;
+    const int E = r < rows ? exps[r] : 0;
+    constexpr uint32_t NEG = 0x80808080u;
+    const int64_t pitch = 2 * kh;
+    const double* Xd = reinterpret_cast<const double*>(X);
+    // the real parts, then the imaginary parts (each pass as the real split)
+#pragma unroll 1
+    for (int part = 0; part < 2; ++part) {
+        uint32_t pk[S][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int dg[4][S];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int64_t l = l0 + q * 4 + e;
+                double x = 0.0;
+                if (r < rows && l < k) x = Xd[2 * (KCONTIG ? l + r * ld : r + l * ld) + part];
+                digits_of<S>(x, E, dg[e]);
+            }
+#pragma unroll
+            for (int s = 0; s < S; ++s) pk[s][q] = pack4_e4m3(dg[0][s], dg[1][s], dg[2][s], dg[3][s]);
+        }
+        const uint32_t flip = part ? conj_mask : 0u;  // the sign of a conjugated imaginary part
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            uint8_t* base = out + (int64_t)s * slice_rows * pitch;
+            const uint4 v = make_uint4(pk[s][0] ^ flip, pk[s][1] ^ flip, pk[s][2] ^ flip, pk[s][3] ^ flip);
+            if (!BSIDE) {
+                *reinterpret_cast<uint4*>(base + r * pitch + part * kh + l0) = v;
+            } else if (part == 0) {  // Re b: first half of row r, second half of row half_rows + r
+                *reinterpret_cast<uint4*>(base + r * pitch + l0) = v;
+                *reinterpret_cast<uint4*>(base + (rows_pad + r) * pitch + kh + l0) = v;
+            } else {  // Im b: negated in row r, as is in row half_rows + r
+                const uint4 nv = make_uint4(v.x ^ NEG, v.y ^ NEG, v.z ^ NEG, v.w ^ NEG);
+                *reinterpret_cast<uint4*>(base + r * pitch + kh + l0) = nv;
+                *reinterpret_cast<uint4*>(base + (rows_pad + r) * pitch + l0) = v;
+            }
+        }
     }
 }
 
@@ -429,10 +502,15 @@ __device__ __forceinline__ bool epilogue_tile(const GemmParams& p, int mb, int n
                 if (g < last) {
                     tc::st_u128_hint(wp + j * BM, make_ulonglong2(lo, hi), pol_keep);
                 } else {
-                    const int64_t gj = (int64_t)nb * BN + col;
+                    int64_t gj = (int64_t)nb * BN + col;
+                    int part = 0;
+                    if (gj >= p.n_split) {
+                        gj -= p.n_split;
+                        part = 1;
+                    }
                     if (gi < p.m && gj < p.n) {
                         double r = i128_to_double(lo, hi, Ei + p.expB[gj] - p.L);
-                        double* cp = p.C + gi + gj * p.ldc;
+                        double* cp = p.C + (gi + gj * p.ldc) * p.cs + part;
                         // C = fl(fl(alpha*r) + fl(beta*C)), no contraction
                         if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
                         if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
@@ -771,6 +849,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // ------------------------------------------------------------------ host
 struct Workspace {
     DeviceBuffer slicesA, slicesB, expA, expB, part, W, stats, err;
+    DeviceBuffer T;  // complex alpha/beta: the product before alpha*T + beta*C
     Stats* host_stats = nullptr;
     unsigned* host_err = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // prep start/end, gemm start/end
@@ -871,12 +950,16 @@ void split(int S, bool kcontig, const double* X, int64_t ld, int64_t rows, int64
     }
 }
 
-// Row scaling of a (rows x k) operand; kcontig as in split_kernel.
+// Row scaling of a (rows x k) operand; kcontig as in split_kernel.  es = 2
+// for complex operands (ld in complex elements): a row's exponent covers the
+// real and imaginary parts, and the spread is measured over 2k terms.
 int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, int* exps, Workspace* w,
-               Stats* st_dev, int which, cudaStream_t st) {
+               Stats* st_dev, int which, cudaStream_t st, int es = 1) {
     if (rows == 0) return COSMA_GPU_SUCCESS;
     if (kcontig) {
-        scale_kcontig_kernel<<<(unsigned)ceil_div(rows, 8), 256, 0, st>>>(X, ld, rows, k, exps, st_dev, which);
+        // a complex row is 2k consecutive doubles
+        scale_kcontig_kernel<<<(unsigned)ceil_div(rows, 8), 256, 0, st>>>(X, ld * es, rows, k * es, exps, st_dev,
+                                                                          which);
     } else {
         const int64_t row_blocks = ceil_div(rows, 256);
         int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
@@ -886,9 +969,9 @@ int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t 
         int* pe = (int*)w->part.ptr;
         float* pm = (float*)((char*)w->part.ptr + (size_t)nchunks * rows * 4);
         scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
-            X, ld, rows, k, kchunk, pe, pm, st_dev);
-        scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, rows, k, exps, st_dev,
-                                                                            which);
+            X, ld * es, es, rows, k, kchunk, pe, pm, st_dev);
+        scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, rows, k * es, exps,
+                                                                            st_dev, which);
     }
     CGB_CUDA(cudaGetLastError());
     return COSMA_GPU_SUCCESS;
@@ -1069,6 +1152,8 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
     CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &L));
     set_tiles(shape, p);
     p.m = m; p.n = n; p.ldc = g.ldc;
+    p.n_split = INT64_MAX;
+    p.cs = 1;
     p.C = (double*)g.C;
     p.expA = (const int*)w->expA.ptr;
     p.expB = (const int*)w->expB.ptr;
@@ -1106,6 +1191,157 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
     return COSMA_GPU_SUCCESS;
 }
 
+template <int S>
+void launch_split_cplx(bool kcontig, bool bside, const double2* X, int64_t ld, int64_t rows, int64_t k,
+                       const int* exps, int64_t kh, int64_t rows_pad, int64_t slice_rows, uint32_t conj_mask,
+                       uint8_t* out, cudaStream_t st) {
+    dim3 grid((unsigned)(rows_pad / 64), (unsigned)(kh / 64));
+#define CGB_SPLITC(KC, BS)                                                                                       \
+    split_cplx_kernel<S, KC, BS><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj_mask, \
+                                                       out)
+    if (kcontig) {
+        if (bside) CGB_SPLITC(true, true); else CGB_SPLITC(true, false);
+    } else {
+        if (bside) CGB_SPLITC(false, true); else CGB_SPLITC(false, false);
+    }
+#undef CGB_SPLITC
+}
+
+void split_cplx(int S, bool kcontig, bool bside, const double2* X, int64_t ld, int64_t rows, int64_t k,
+                const int* exps, int64_t kh, int64_t rows_pad, int64_t slice_rows, bool conj, uint8_t* out,
+                cudaStream_t st) {
+    const uint32_t cm = conj ? 0x80808080u : 0u;
+    switch (S) {
+#define CGB_SPLIT_CASE(n) \
+    case n: launch_split_cplx<n>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, cm, out, st); break;
+        CGB_SPLIT_CASE(2) CGB_SPLIT_CASE(3) CGB_SPLIT_CASE(4) CGB_SPLIT_CASE(5) CGB_SPLIT_CASE(6) CGB_SPLIT_CASE(7)
+        CGB_SPLIT_CASE(8) CGB_SPLIT_CASE(9) CGB_SPLIT_CASE(10) CGB_SPLIT_CASE(11) CGB_SPLIT_CASE(12)
+        CGB_SPLIT_CASE(13) CGB_SPLIT_CASE(14) CGB_SPLIT_CASE(15) CGB_SPLIT_CASE(16)
+#undef CGB_SPLIT_CASE
+        default: break;
+    }
+}
+
+// Shape of the complex form: the GEMM has 2*nh columns (real parts, then
+// imaginary parts), nh = n padded to 256; both halves must tile exactly.
+GemmShape cplx_shape(int64_t m, int64_t n, int64_t* nh_out) {
+    const int64_t nh = ceil_div(n, BN) * BN;
+    GemmShape sh = gemm_shape(m, 2 * nh);
+    if (sh.n_pad != 2 * nh) {  // 2*nh/256 tiles is even: clusters of 2 tile it exactly
+        sh.cl = 2;
+        sh.n_pad = 2 * nh;
+    }
+    *nh_out = nh;
+    return sh;
+}
+
+// One complex pass with 2k <= MAX_K_PER_CALL: the same pipeline on the
+// concatenated real operands (4 real products per complex one, "4M").
+int ozaki_zchunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_info* info) {
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const bool a_kc = g.opa != 0, b_kc = g.opb == 0;
+    const double2* A = (const double2*)g.A;
+    const double2* B = (const double2*)g.B;
+    Workspace* w = workspace(st);
+    if (!w->host_stats || !w->host_err) return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "ozaki: pinned staging");
+    int64_t nh = 0;
+    const GemmShape shape = cplx_shape(m, n, &nh);
+    const int64_t m_pad = shape.m_pad, kh = ceil_div(k, 64) * 64, k_pad = 2 * kh;
+
+    // 1. scaling over both parts of every row / column
+    CGB_CHECK(w->stats.reserve(sizeof(Stats), st));
+    CGB_CHECK(w->err.reserve(sizeof(unsigned), st));
+    CGB_CHECK(w->expA.reserve((size_t)m_pad * 4, st));
+    CGB_CHECK(w->expB.reserve((size_t)nh * 4, st));
+    Stats* st_dev = (Stats*)w->stats.ptr;
+    if (!w->ev[0] || !w->ev[3]) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki: timing events");
+    CGB_CUDA(cudaEventRecord(w->ev[0], st));
+    CGB_CUDA(cudaMemsetAsync(st_dev, 0, sizeof(Stats), st));
+    CGB_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(unsigned), st));
+    CGB_CUDA(cudaMemsetAsync(w->expA.ptr, 0, (size_t)m_pad * 4, st));
+    CGB_CUDA(cudaMemsetAsync(w->expB.ptr, 0, (size_t)nh * 4, st));
+    CGB_CHECK(scale_rows(a_kc, (const double*)A, g.lda, m, k, (int*)w->expA.ptr, w, st_dev, 0, st, 2));
+    CGB_CHECK(scale_rows(b_kc, (const double*)B, g.ldb, n, k, (int*)w->expB.ptr, w, st_dev, 1, st, 2));
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, st_dev, sizeof(Stats), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    const Stats hs = *w->host_stats;
+    const double spread = (double)hs.spread[0] + (double)hs.spread[1];
+    if (hs.nonfinite) {
+        if (info) info->fallback_native = 1;
+        return native_gemm(g, st);
+    }
+    const int S = slices > 0 ? std::min(slices, MAX_SLICES) : choose_slices(spread, 2 * k);
+    if (S < 2) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki: at least 2 slices");
+
+    // 2. slices of [Re | Im] rows of op(A) and of the two stacked forms of op(B)
+    CGB_CHECK(w->slicesA.reserve((size_t)S * m_pad * k_pad, st));
+    CGB_CHECK(w->slicesB.reserve((size_t)S * 2 * nh * k_pad, st));
+    split_cplx(S, a_kc, false, A, g.lda, m, k, (const int*)w->expA.ptr, kh, m_pad, m_pad, g.opa == 2,
+               (uint8_t*)w->slicesA.ptr, st);
+    split_cplx(S, b_kc, true, B, g.ldb, n, k, (const int*)w->expB.ptr, kh, nh, 2 * nh, g.opb == 2,
+               (uint8_t*)w->slicesB.ptr, st);
+    CGB_CUDA(cudaGetLastError());
+    CGB_CUDA(cudaEventRecord(w->ev[1], st));
+
+    // 3. slice products; real alpha and beta are applied in the epilogue,
+    //    complex ones by alpha*T + beta*C afterwards
+    const bool fused = g.alpha[1] == 0.0 && g.beta[1] == 0.0;
+    GemmParams p;
+    std::memset(&p, 0, sizeof(p));
+    int L = 0;
+    CGB_CHECK(build_schedule(S, 2 * k, k_pad, (int)m_pad, (int)(2 * nh), &p.sched, &L));
+    set_tiles(shape, p);
+    p.m = m;
+    p.n = n;
+    p.n_split = nh;
+    p.cs = 2;
+    if (fused) {
+        p.C = (double*)g.C;
+        p.ldc = g.ldc;
+        p.alpha = g.alpha[0];
+        p.beta = g.beta[0];
+    } else {
+        CGB_CHECK(w->T.reserve((size_t)m * n * 16, st));
+        p.C = (double*)w->T.ptr;
+        p.ldc = m;
+        p.alpha = 1.0;
+        p.beta = 0.0;
+    }
+    p.beta_zero = p.beta == 0.0;
+    p.alpha_one = p.alpha == 1.0;
+    p.expA = (const int*)w->expA.ptr;
+    p.expB = (const int*)w->expB.ptr;
+    p.L = L;
+    int grid = 0;
+    CGB_CHECK(gemm_grid(shape, p.num_tiles, &grid));
+    CGB_CHECK(w->W.reserve((size_t)grid * BM * BN * sizeof(ulonglong2), st));
+    p.W = (ulonglong2*)w->W.ptr;
+    p.err = (unsigned*)w->err.ptr;
+    CGB_CUDA(cudaEventRecord(w->ev[2], st));
+    CGB_CHECK(launch_slice_gemm(shape, grid, w->slicesA.ptr, w->slicesB.ptr, S, k_pad, p, st));
+    CGB_CUDA(cudaEventRecord(w->ev[3], st));
+    CGB_CUDA(cudaMemcpyAsync(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    if (*w->host_err)
+        return set_error(COSMA_GPU_ERROR_DEVICE_TIMEOUT,
+                         "ozaki gemm: a pipeline wait timed out (device code " + std::to_string(*w->host_err) + ")");
+    if (!fused) CGB_CHECK(unpack_device(Scalar::Z, m, n, g.alpha, w->T.ptr, m, g.beta, g.C, g.ldc, st));
+    if (info) {
+        int products = 0;
+        for (int i = 0; i < p.sched.n_groups; ++i) products += p.sched.gcount[i];
+        float prep = 0.f, gemm = 0.f;
+        cudaEventElapsedTime(&prep, w->ev[0], w->ev[1]);
+        cudaEventElapsedTime(&gemm, w->ev[2], w->ev[3]);
+        info->slices = S;
+        info->products = products;
+        info->groups = p.sched.n_groups;
+        info->spread_bits = spread;
+        info->prep_ms += prep;
+        info->gemm_ms += gemm;
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
 }  // namespace oz
 
 int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
@@ -1125,6 +1361,26 @@ int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
         if (k0 > 0) { c.beta[0] = 1.0; c.beta[1] = 0.0; }
         // a chunk holding Inf/NaN runs on the native kernel; the others stay split
         CGB_CHECK(oz::ozaki_chunk(c, slices, stream, info));
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+int ozaki_zgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
+    if (g.scalar != Scalar::Z) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: complex double only");
+    if (((uintptr_t)g.A | (uintptr_t)g.B | (uintptr_t)g.C) % 16)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: complex buffers must be 16-byte aligned");
+    if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 23)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: m is limited to 2^24 and n to 2^23 (complex)");
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    // each complex term is two real terms: half the real pass length per chunk
+    const int64_t kmax = oz::MAX_K_PER_CALL / 2;
+    GemmDesc c = g;
+    for (int64_t k0 = 0; k0 < g.k; k0 += kmax) {
+        c.k = std::min<int64_t>(kmax, g.k - k0);
+        c.A = (const double2*)g.A + (g.opa == 0 ? k0 * g.lda : k0);
+        c.B = (const double2*)g.B + (g.opb == 0 ? k0 : k0 * g.ldb);
+        if (k0 > 0) { c.beta[0] = 1.0; c.beta[1] = 0.0; }
+        CGB_CHECK(oz::ozaki_zchunk(c, slices, stream, info));
     }
     return COSMA_GPU_SUCCESS;
 }
@@ -1257,7 +1513,7 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
             int* pe = (int*)part;
             float* pm = (float*)(part + (size_t)nchunks * o.rows * 4);
             scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
-                o.X, o.ld, o.rows, k, kchunk, pe, pm, st_dev);
+                o.X, o.ld, 1, o.rows, k, kchunk, pe, pm, st_dev);
             scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, o.rows, k, o.exps,
                                                                                 st_dev, o.which);
         }
@@ -1291,6 +1547,8 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
     CGB_CHECK(build_schedule(S, k, k_pad, (int)m_pad, (int)n_pad, &p.sched, &Lw));
     set_tiles(shape, p);
     p.m = m; p.n = n; p.ldc = g.ldc;
+    p.n_split = INT64_MAX;
+    p.cs = 1;
     p.C = (double*)g.C;
     p.expA = expA;
     p.expB = expB;

@@ -68,6 +68,10 @@ int scale_matrix_device(Scalar s, int64_t rows, int64_t cols, const double* beta
                         int64_t ldc, cudaStream_t stream);        // layout.cu
 int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream,
                 cosma_gpu_ozaki_info* info);                     // ozaki.cu
+int ozaki_zgemm(const GemmDesc& g, int slices, cudaStream_t stream,
+                cosma_gpu_ozaki_info* info);                     // ozaki.cu
+int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
+                  const double* beta, void* dst, int64_t ldd, cudaStream_t s);  // layout.cu
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
 
 // Dispatches one device-pointer GEMM by method (handles the k == 0 /

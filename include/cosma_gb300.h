@@ -157,6 +157,14 @@ int cosma_gpu_dgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n,
                                  double alpha, const double* A, int64_t lda, const double* B,
                                  int64_t ldb, double beta, double* C, int64_t ldc, int slices,
                                  void* stream, cosma_gpu_ozaki_info* info);
+/* The same for complex double (interleaved re/im, op N, T or C): the real
+ * and imaginary parts come out of one slice-product GEMM over [Re | Im]
+ * digit rows (four real products per complex one), each part summed exactly
+ * and rounded once.  alpha/beta point to {re, im}. */
+int cosma_gpu_zgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                 const double* alpha, const double* A, int64_t lda,
+                                 const double* B, int64_t ldb, const double* beta, double* C,
+                                 int64_t ldc, int slices, void* stream, cosma_gpu_ozaki_info* info);
 
 /* Size of the static device array that cosma_gpu_dgemm_ozaki_noalloc draws
  * all of its scratch from (64 MiB, held on every GPU that loads the library). */

@@ -30,7 +30,7 @@ def test_header_declares_the_drop_in_surface():
     names = declared_symbols()
     for must in ["pdgemm_", "pzgemm_", "psgemm", "PDGEMM_", "cosma_pdgemm", "COSMA_PZGEMM_",
                  "cosma_gpu_tmm_gemm_d", "cosma_gpu_tmm_make_context", "cosma_gpu_local_multiply_d",
-                 "cosma_gpu_dgemm_ozaki_device", "costa_gpu_pack", "costa_gpu_unpack_d"]:
+                 "cosma_gpu_dgemm_ozaki_device", "cosma_gpu_zgemm_ozaki_device", "costa_gpu_pack", "costa_gpu_unpack_d"]:
         assert must in names, must
 
 

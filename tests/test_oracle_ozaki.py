@@ -85,3 +85,19 @@ def test_sampled_restatement_matches_full():
         rows = rng.integers(0, m, 60)
         cols = rng.integers(0, n, 60)
         np.testing.assert_array_equal(ozaki.ozaki_gemm_sampled(ta, tb, A, B, S, rows, cols), full[rows, cols])
+
+
+def test_complex_restatement_is_the_complex_product():
+    rng = np.random.default_rng(4)
+    for ta, tb in (("N", "N"), ("T", "C"), ("C", "T")):
+        m, n, k = 13, 11, 19
+        sa = (m, k) if ta == "N" else (k, m)
+        sb = (k, n) if tb == "N" else (n, k)
+        A = rng.uniform(-1, 1, sa) + 1j * rng.uniform(-1, 1, sa)
+        B = rng.uniform(-1, 1, sb) + 1j * rng.uniform(-1, 1, sb)
+        opA = A if ta == "N" else (A.T if ta == "T" else A.conj().T)
+        opB = B if tb == "N" else (B.T if tb == "T" else B.conj().T)
+        got = ozaki.ozaki_zgemm(ta, tb, A, B, 13)
+        np.testing.assert_allclose(got, opA @ opB, rtol=0, atol=1e-14)
+        rows, cols = rng.integers(0, m, 30), rng.integers(0, n, 30)
+        np.testing.assert_array_equal(ozaki.ozaki_zgemm_sampled(ta, tb, A, B, 13, rows, cols), got[rows, cols])
