@@ -80,6 +80,7 @@ SIGNATURES = {
     "cosma_gpu_grouped_plan_create": (vp, [i32, i32, C.POINTER(GemmProblem), i32, vp]),
     "cosma_gpu_grouped_plan_run": (i32, [vp, vp]),
     "cosma_gpu_grouped_plan_info": (i32, [vp, C.POINTER(GroupedInfo)]),
+    "cosma_gpu_grouped_plan_slices": (i32, [vp, C.POINTER(C.c_int)]),
     "cosma_gpu_grouped_plan_destroy": (None, [vp]),
     "cosma_gpu_dgemm_grouped_device": (i32, [i32, i32, C.POINTER(GemmProblem), vp]),
     "costa_gpu_pack": (i32, [ch, i32, i32, i64, i64, vp, i64, vp, i64, vp]),

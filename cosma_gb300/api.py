@@ -216,7 +216,7 @@ def zgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm,
 
 class GroupedPlan:
     """A grouped FP64 GEMM over many device problems, one persistent launch
-    replayed from a CUDA graph.  `problems` is a list of tuples
+    replayed from a CUDA graph (method "native" or "ozaki").  `problems` is a list of tuples
     (transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) with device
     buffers (torch tensors or raw addresses)."""
 
@@ -238,6 +238,12 @@ class GroupedPlan:
         inf = N.GroupedInfo()
         N.check(self.lib.cosma_gpu_grouped_plan_info(self._p, C.byref(inf)))
         return inf.as_dict()
+
+    def slices(self):
+        """Planned slice count per problem (Ozaki plans; 0 where not sliced)."""
+        out = (C.c_int * max(1, len(self._keep)))()
+        N.check(self.lib.cosma_gpu_grouped_plan_slices(self._p, out))
+        return list(out)[:len(self._keep)]
 
     def close(self):
         if self._p:

@@ -186,6 +186,7 @@ struct cosma_gpu_grouped_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t capture_stream = nullptr;
+    cosma_gpu_oz_grouped_plan* oz = nullptr;  // the Ozaki-split form, when chosen
 };
 
 namespace cgb {
@@ -359,13 +360,24 @@ cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count, con
                                                       int autotune, void* stream) {
     using namespace cgb;
     clear_error();
-    if (method != COSMA_GPU_METHOD_AUTO && method != COSMA_GPU_METHOD_NATIVE) {
-        set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "grouped: only the native FP64 method is implemented");
+    if (method != COSMA_GPU_METHOD_AUTO && method != COSMA_GPU_METHOD_NATIVE && method != COSMA_GPU_METHOD_OZAKI) {
+        set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "grouped: the native FP64 and Ozaki methods are implemented");
         return nullptr;
     }
     if (count < 0 || (count > 0 && !problems)) {
         set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: bad problem array");
         return nullptr;
+    }
+    if (method == COSMA_GPU_METHOD_OZAKI) {
+        auto* pl = new cosma_gpu_grouped_plan();
+        pl->count = count;
+        int s = COSMA_GPU_SUCCESS;
+        pl->oz = oz_grouped_create(count, problems, autotune, (cudaStream_t)stream, &s);
+        if (!pl->oz) {
+            delete pl;
+            return nullptr;
+        }
+        return pl;
     }
     auto* pl = new cosma_gpu_grouped_plan();
     cudaStream_t st = (cudaStream_t)stream;
@@ -408,6 +420,7 @@ cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count, con
 int cosma_gpu_grouped_plan_run(cosma_gpu_grouped_plan* pl, void* stream) {
     cgb::clear_error();
     if (!pl) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: null plan");
+    if (pl->oz) return cgb::oz_grouped_run(pl->oz, (cudaStream_t)stream);
     if (pl->ntiles == 0) return COSMA_GPU_SUCCESS;
     CGB_CUDA(cudaGraphLaunch(pl->exec, (cudaStream_t)stream));
     return COSMA_GPU_SUCCESS;
@@ -415,6 +428,10 @@ int cosma_gpu_grouped_plan_run(cosma_gpu_grouped_plan* pl, void* stream) {
 
 int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* pl, cosma_gpu_grouped_info* info) {
     if (!pl || !info) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: null argument");
+    if (pl->oz) {
+        cgb::oz_grouped_info(pl->oz, info);
+        return COSMA_GPU_SUCCESS;
+    }
     info->tiles = pl->ntiles;
     info->tile_policy = pl->cfg.policy;
     info->dynamic_schedule = pl->cfg.dynamic_sched;
@@ -425,8 +442,16 @@ int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* pl, cosma_gpu_grouped_in
     return COSMA_GPU_SUCCESS;
 }
 
+int cosma_gpu_grouped_plan_slices(cosma_gpu_grouped_plan* pl, int* slices) {
+    if (!pl || !slices) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: null argument");
+    if (pl->oz) return cgb::oz_grouped_slices(pl->oz, slices);
+    for (int i = 0; i < pl->count; ++i) slices[i] = 0;
+    return COSMA_GPU_SUCCESS;
+}
+
 void cosma_gpu_grouped_plan_destroy(cosma_gpu_grouped_plan* pl) {
     if (!pl) return;
+    if (pl->oz) cgb::oz_grouped_destroy(pl->oz);
     if (pl->exec) cudaGraphExecDestroy(pl->exec);
     if (pl->graph) cudaGraphDestroy(pl->graph);
     if (pl->capture_stream) cudaStreamDestroy(pl->capture_stream);

@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <cstdint>
 
+struct cosma_gpu_oz_grouped_plan;  // grouped Ozaki plan (ozaki_grouped.cu)
+
 namespace cgb {
 
 bool env_bool(const char* name, bool dflt);
@@ -73,6 +75,15 @@ int ozaki_zgemm(const GemmDesc& g, int slices, cudaStream_t stream,
 int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
                   const double* beta, void* dst, int64_t ldd, cudaStream_t s);  // layout.cu
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
+
+// Grouped Ozaki-split FP64 GEMM (ozaki_grouped.cu), driven by the grouped
+// plan of grouped.cu when it is created with the Ozaki method.
+cosma_gpu_oz_grouped_plan* oz_grouped_create(int count, const cosma_gpu_gemm_problem* problems, int autotune,
+                                             cudaStream_t st, int* status);
+int oz_grouped_run(cosma_gpu_oz_grouped_plan* pl, cudaStream_t st);
+void oz_grouped_destroy(cosma_gpu_oz_grouped_plan* pl);
+void oz_grouped_info(const cosma_gpu_oz_grouped_plan* pl, cosma_gpu_grouped_info* info);
+int oz_grouped_slices(const cosma_gpu_oz_grouped_plan* pl, int* out);
 
 // Dispatches one device-pointer GEMM by method (handles the k == 0 /
 // alpha == 0 corner cases).  Defined in gemm_dispatch.cpp.

@@ -221,14 +221,25 @@ typedef struct cosma_gpu_grouped_info {
  * schedule and CTA size are chosen by timing candidates on the batch (the
  * choice is cached per batch signature); tuning runs the batch several times
  * and restores the C of problems with beta != 0.  The problem array is copied;
- * the device buffers must stay valid while the plan is used. */
+ * the device buffers must stay valid while the plan is used.
+ *
+ * method COSMA_GPU_METHOD_OZAKI gives the FP64-accurate form: the graph
+ * scales, slices and multiplies every problem on the FP8 tensor cores (one
+ * launch per step over the whole batch).  Slice counts are planned from the
+ * data present at creation and re-checked on the device at every run; a
+ * problem whose data then needs more slices, or holds Inf/NaN, is left to the
+ * single-problem path.  Runs of an Ozaki plan synchronise `stream` (the host
+ * reads the check), and tuning (tile order) runs only for beta == 0 batches. */
 typedef struct cosma_gpu_grouped_plan cosma_gpu_grouped_plan;
 cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count,
                                                       const cosma_gpu_gemm_problem* problems,
                                                       int autotune, void* stream);
-/* Replays the plan's CUDA graph on `stream` (asynchronous). */
+/* Replays the plan's CUDA graph on `stream` (asynchronous for native plans). */
 int cosma_gpu_grouped_plan_run(cosma_gpu_grouped_plan* plan, void* stream);
 int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* plan, cosma_gpu_grouped_info* info);
+/* Slice count planned for each problem of an Ozaki plan (`count` ints; 0 for
+ * problems the plan does not slice, and for every problem of a native plan). */
+int cosma_gpu_grouped_plan_slices(cosma_gpu_grouped_plan* plan, int* slices);
 void cosma_gpu_grouped_plan_destroy(cosma_gpu_grouped_plan* plan);
 /* One-shot grouped GEMM (plan without tuning, run, synchronise, destroy). */
 int cosma_gpu_dgemm_grouped_device(int method, int count, const cosma_gpu_gemm_problem* problems,
