@@ -46,8 +46,11 @@ int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t st
     if (method == COSMA_GPU_METHOD_OZAKI) {
         if (g.scalar == Scalar::D) return ozaki_dgemm(g, ozaki_slices, stream, info);
         if (g.scalar == Scalar::Z) return ozaki_zgemm(g, ozaki_slices, stream, info);
-        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED,
-                         "gemm: the Ozaki method is implemented for double and complex double");
+        // single precision: the tensor-core form accurate to FP32 (real), or
+        // the native kernel (complex), so that a process-wide Ozaki default
+        // also serves psgemm / pcgemm callers
+        if (g.scalar == Scalar::S) return bf16x3_sgemm(g, stream);
+        return native_gemm(g, stream);
     }
     if (method == COSMA_GPU_METHOD_BF16X3) {
         if (g.scalar == Scalar::S) return bf16x3_sgemm(g, stream);

@@ -9,9 +9,10 @@
 //   2. a check that recomputes each problem's slice count from its spread and
 //      compares it with the count the plan was built for;
 //   3. digit slicing (one launch per slice count and memory order);
-//   4. one persistent slice-product GEMM over the tiles of all problems:
-//      the single-CTA tcgen05 kind::f8f6f4 pipeline of ozaki.cu, with a
-//      tensor map, schedule and output description per problem.
+//   4. one persistent slice-product GEMM over the 128 x 64 tiles of all
+//      problems: the warp-specialised tcgen05 kind::f8f6f4 pipeline of
+//      ozaki.cu with the 128-bit partial sums held in TMEM, and a tensor map,
+//      schedule and output description per problem.
 // A problem whose data needs more slices than planned (or holds Inf/NaN) is
 // skipped by steps 3-4, its C untouched, and recomputed by the host on the
 // single-problem path, so a replay never returns a less accurate result.
@@ -57,17 +58,6 @@ struct Prob {
     uint8_t* slB;
 };
 
-// Output description handed to the shared epilogue.
-struct EpiView {
-    int64_t m, n, ldc, n_split;
-    int cs;
-    double* C;
-    const int* expA;
-    const int* expB;
-    double alpha, beta;
-    int alpha_one, beta_zero, L;
-    unsigned* err;
-};
 
 // Items of the prep launches: {problem, operand (0 A, 1 B), block x, block y}.
 using Item = int4;
@@ -173,7 +163,92 @@ __global__ void __launch_bounds__(256) gsplit_kernel(const Prob* __restrict__ P,
     else split_block<S, KCONTIG>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n_pad, p.slB, it.z, it.w);
 }
 
-// Persistent slice-product GEMM over the 128 x 256 tiles of every problem
+// Tiles of the grouped GEMM: 128 x 64.  Batches hold many small problems,
+// for which a 128 x 256 tile wastes work on padding and, above all, spends
+// its time draining accumulators into 128-bit partial sums in global memory
+// (one drain per accumulator group, ~14 per tile, each a round trip to L2).
+// At N = 64 the partial sums of a tile fit in TMEM beside two accumulators:
+//   columns [0, 64) and [64, 128): FP32 accumulators (double-buffered)
+//   columns [128 + 64w, 192 + 64w), w = 0..3: 32-bit word w of the 128-bit
+//   partial sum of each of the 64 tile columns
+// so a drain never leaves the SM.  The B slab of a stage shrinks to 8 KB, and
+// eight 24 KB stages fit in shared memory.
+constexpr int GBN = 64;
+constexpr int G_STAGES = 8;
+constexpr int G_A = BM * BK, G_B = GBN * BK, G_STAGE = G_A + G_B;
+constexpr int G_SMEM = G_STAGES * G_STAGE + 1024 + 256;
+constexpr uint32_t G_WCOL = 2 * GBN;
+static_assert(G_WCOL + 4 * GBN <= 512, "TMEM columns");
+
+// Drains the accumulator groups of one tile (rows mb*128.., columns
+// nb*64..) into the TMEM partial sums and, after the last group, rounds them
+// to FP64 and writes alpha*r + beta*C.
+template <class Release>
+__device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc, int mb, int nb, uint32_t tmem,
+                                               int quad, int lane, uint64_t* accf, uint32_t& acc_it,
+                                               uint64_t pol_stream, unsigned* err, Release release) {
+    const int row = quad * 32 + lane;
+    const int64_t gi = (int64_t)mb * BM + row;
+    const int Ei = p.expA[gi];
+    const uint32_t lanes = (uint32_t)(quad * 32) << 16;
+    const int last = sc.n_groups - 1;
+    for (int g = 0; g <= last; ++g, ++acc_it) {
+        const uint32_t buf = acc_it & 1;
+        if (!__all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, err, kDevTimeoutAcc)))
+            return false;
+        tc::tc_fence_after();
+        const int sh = sc.gshift[g];
+#pragma unroll 1
+        for (int c = 0; c < GBN; c += 16) {
+            uint32_t v[16], w0[16], w1[16], w2[16], w3[16];
+            tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c, v);
+            if (g > 0) {
+                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 0 * GBN + c, w0);
+                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 1 * GBN + c, w1);
+                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 2 * GBN + c, w2);
+                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 3 * GBN + c, w3);
+            }
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int x = __float2int_rn(__uint_as_float(v[j]));
+                unsigned long long lo = 0, hi = 0;
+                if (g > 0) {
+                    lo = ((unsigned long long)w1[j] << 32) | w0[j];
+                    hi = ((unsigned long long)w3[j] << 32) | w2[j];
+                }
+                add_shifted(lo, hi, x, sh);
+                if (g < last) {
+                    w0[j] = (uint32_t)lo;
+                    w1[j] = (uint32_t)(lo >> 32);
+                    w2[j] = (uint32_t)hi;
+                    w3[j] = (uint32_t)(hi >> 32);
+                } else {
+                    const int64_t gj = (int64_t)nb * GBN + c + j;
+                    if (gi < p.m && gj < p.n) {
+                        double r = i128_to_double(lo, hi, Ei + p.expB[gj] - p.L);
+                        double* cp = p.C + gi + gj * p.ldc;
+                        if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
+                        if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+                        tc::st_f64_hint(cp, r, pol_stream);
+                    }
+                }
+            }
+            if (g < last) {
+                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 0 * GBN + c, w0);
+                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 1 * GBN + c, w1);
+                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 2 * GBN + c, w2);
+                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 3 * GBN + c, w3);
+            }
+        }
+        if (g < last) tc::tmem_st_wait();
+        tc::tc_fence_before();
+        release(buf);
+    }
+    return true;
+}
+
+// Persistent slice-product GEMM over the 128 x 64 tiles of every problem
 // ({problem, m block, n block} in `tiles`, taken round-robin by the CTAs).
 // The roles are those of ozaki_gemm_kernel<1>; per tile they switch to the
 // problem's tensor maps (maps[2i], maps[2i+1] in global memory), schedule
@@ -182,19 +257,19 @@ __global__ void __launch_bounds__(256) gsplit_kernel(const Prob* __restrict__ P,
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_grouped_gemm_kernel(const Prob* __restrict__ P, const CUtensorMap* __restrict__ maps,
                               const Schedule* __restrict__ scheds, const int4* __restrict__ tiles, int ntiles,
-                              const int* __restrict__ okf, ulonglong2* __restrict__ Wbase, unsigned* err) {
+                              const int* __restrict__ okf, unsigned* err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
-    uint64_t* empty = full + STAGES;
-    uint64_t* accf = empty + STAGES;
+    uint64_t* full = (uint64_t*)(smem + G_STAGES * G_STAGE);
+    uint64_t* empty = full + G_STAGES;
+    uint64_t* accf = empty + G_STAGES;
     uint64_t* acce = accf + 2;
     uint64_t* drain = acce + 2;
     uint32_t* tmem_slot = (uint32_t*)(drain + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < G_STAGES; ++s) {
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
@@ -228,28 +303,28 @@ __global__ void __launch_bounds__(THREADS, 1)
                         const int kc1 = min(p.kb_count, kc + KB_CHUNK);
                         for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
                             const int arow = sc.us[u] * p.m_pad + tl.y * BM;
-                            const int brow = sc.ut[u] * p.n_pad + tl.z * BN;
+                            const int brow = sc.ut[u] * p.n_pad + tl.z * GBN;
                             for (int kb = kc; kb < kc1; ++kb, ++it) {
-                                const int st = it % STAGES;
-                                if (!tc::mbar_wait(&empty[st], ((it / STAGES) & 1) ^ 1, err, kDevTimeoutEmpty)) {
+                                const int st = it % G_STAGES;
+                                if (!tc::mbar_wait(&empty[st], ((it / G_STAGES) & 1) ^ 1, err, kDevTimeoutEmpty)) {
                                     ok = false;
                                     break;
                                 }
-                                tc::mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
-                                uint8_t* sa = smem + st * STAGE_BYTES;
+                                tc::mbar_arrive_expect_tx(&full[st], G_STAGE);
+                                uint8_t* sa = smem + st * G_STAGE;
                                 tc::tma_load_2d(sa, tmA, kb * BK, arow, &full[st]);
-                                tc::tma_load_2d(sa + A_STAGE, tmB, kb * BK, brow, &full[st]);
+                                tc::tma_load_2d(sa + G_A, tmB, kb * BK, brow, &full[st]);
                             }
                         }
                     }
                 }
             }
-            const uint32_t first = it > STAGES ? it - STAGES : 0;
-            for (uint32_t j = first; j < it; ++j) tc::mbar_wait_drain(&full[j % STAGES], (j / STAGES) & 1);
+            const uint32_t first = it > G_STAGES ? it - G_STAGES : 0;
+            for (uint32_t j = first; j < it; ++j) tc::mbar_wait_drain(&full[j % G_STAGES], (j / G_STAGES) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---------------------------------- MMA issuer
-            constexpr uint32_t ID = tc::idesc(tc::kFmtE4M3, tc::kFmtE4M3, BM, BN);
+            constexpr uint32_t ID = tc::idesc(tc::kFmtE4M3, tc::kFmtE4M3, BM, GBN);
             uint32_t it = 0, acc_it = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -264,20 +339,20 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     tc::tc_fence_after();
-                    const uint32_t d_tmem = tmem + buf * BN;
+                    const uint32_t d_tmem = tmem + buf * GBN;
                     uint32_t accumulate = 0;
                     for (int kc = 0; kc < p.kb_count && ok; kc += KB_CHUNK) {
                         const int kc1 = min(p.kb_count, kc + KB_CHUNK);
                         for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
                             for (int kb = kc; kb < kc1; ++kb, ++it) {
-                                const int st = it % STAGES;
-                                if (!tc::mbar_wait(&full[st], (it / STAGES) & 1, err, kDevTimeoutFull)) {
+                                const int st = it % G_STAGES;
+                                if (!tc::mbar_wait(&full[st], (it / G_STAGES) & 1, err, kDevTimeoutFull)) {
                                     ok = false;
                                     break;
                                 }
                                 tc::tc_fence_after();
-                                const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES);
-                                const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + A_STAGE);
+                                const uint32_t sa = tc::smem_u32(smem + st * G_STAGE);
+                                const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + G_A);
 #pragma unroll
                                 for (int kk = 0; kk < BK / 32; ++kk) {
                                     tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
@@ -295,30 +370,14 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else {  // ------------------------------------------------ epilogue
         const int quad = warp & 3;
-        ulonglong2* W = Wbase + (size_t)blockIdx.x * (BM * BN);
-        const uint64_t pol_keep = tc::policy_evict_last(), pol_stream = tc::policy_evict_first();
+        const uint64_t pol_stream = tc::policy_evict_first();
         uint32_t acc_it = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int4 tl = tiles[t];
             if (!okf[tl.x]) continue;
             const Prob& p = P[tl.x];
-            EpiView ev;
-            ev.m = p.m;
-            ev.n = p.n;
-            ev.ldc = p.ldc;
-            ev.n_split = INT64_MAX;
-            ev.cs = 1;
-            ev.C = p.C;
-            ev.expA = p.expA;
-            ev.expB = p.expB;
-            ev.alpha = p.alpha;
-            ev.beta = p.beta;
-            ev.alpha_one = p.alpha_one;
-            ev.beta_zero = p.beta_zero;
-            ev.L = p.L;
-            ev.err = err;
-            if (!epilogue_tile(ev, scheds[p.sched], tl.y, tl.z, tmem, quad, lane, W, accf, acc_it, pol_keep,
-                               pol_stream, [&](uint32_t buf) { tc::mbar_arrive(&acce[buf]); }))
+            if (!gepilogue_tile(p, scheds[p.sched], tl.y, tl.z, tmem, quad, lane, accf, acc_it, pol_stream, err,
+                                [&](uint32_t buf) { tc::mbar_arrive(&acce[buf]); }))
                 break;
         }
     }
@@ -364,7 +423,7 @@ struct cosma_gpu_oz_grouped_plan {
     std::vector<Prob> hp;
     std::vector<cosma_gpu_gemm_problem> orig;  // for the host-side recomputation of skipped problems
     std::vector<int> host_side;                // k == 0 or alpha == 0: C <- beta*C on every run
-    cgb::DeviceBuffer probs, maps, scheds, tiles, kitems, mitems, sitems, stats, need, ok, bad, err, exps, slices, W;
+    cgb::DeviceBuffer probs, maps, scheds, tiles, kitems, mitems, sitems, stats, need, ok, bad, err, exps, slices;
     int n_kitems = 0, n_mitems = 0;
     struct SplitLaunch { int S; bool kcontig; int first, count; };
     std::vector<SplitLaunch> splits;
@@ -402,9 +461,9 @@ int enqueue(Plan* pl, cudaStream_t st) {
         gsplit(sl.S, sl.kcontig, sl.count, P, (const Item*)pl->sitems.ptr + sl.first, (const int*)pl->ok.ptr, st);
     CGB_CUDA(cudaGetLastError());
     if (pl->ntiles) {
-        ozaki_grouped_gemm_kernel<<<pl->grid, THREADS, SMEM_BYTES, st>>>(
+        ozaki_grouped_gemm_kernel<<<pl->grid, THREADS, G_SMEM, st>>>(
             P, (const CUtensorMap*)pl->maps.ptr, (const Schedule*)pl->scheds.ptr, (const int4*)pl->tiles.ptr,
-            pl->ntiles, (const int*)pl->ok.ptr, (ulonglong2*)pl->W.ptr, (unsigned*)pl->err.ptr);
+            pl->ntiles, (const int*)pl->ok.ptr, (unsigned*)pl->err.ptr);
         CGB_CUDA(cudaGetLastError());
     }
     return COSMA_GPU_SUCCESS;
@@ -547,7 +606,7 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
         }
         p.S = MAX_SLICES;  // provisional: the planning pass measures what is needed
         p.m_pad = (int)(ceil_div(p.m, BM) * BM);
-        p.n_pad = (int)(ceil_div(p.n, BN) * BN);
+        p.n_pad = (int)(ceil_div(p.n, GBN) * GBN);
         p.k_pad = ceil_div(p.k, BK) * BK;
         p.kb_count = (int)(p.k_pad / BK);
         p.L = 8 + 5 * (p.S - 1);
@@ -636,7 +695,7 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
         CGB_CHECK(make_tmap_2d(&maps[2 * i], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, p.slA, (uint64_t)p.k_pad,
                                (uint64_t)p.S * p.m_pad, (uint64_t)p.k_pad, BK, BM));
         CGB_CHECK(make_tmap_2d(&maps[2 * i + 1], CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, p.slB, (uint64_t)p.k_pad,
-                               (uint64_t)p.S * p.n_pad, (uint64_t)p.k_pad, BK, BN));
+                               (uint64_t)p.S * p.n_pad, (uint64_t)p.k_pad, BK, GBN));
         const int kbk = (int)(p.k_pad / 64);
         auto& ia = sitems[{p.S, p.opa == 1 ? 1 : 0}];
         for (int bx = 0; bx < p.m_pad / 64; ++bx)
@@ -645,7 +704,7 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
         for (int bx = 0; bx < p.n_pad / 64; ++bx)
             for (int by = 0; by < kbk; ++by) ib.push_back(make_int4(i, 1, bx, by));
         for (int mb = 0; mb < p.m_pad / BM; ++mb)
-            for (int nb = 0; nb < p.n_pad / BN; ++nb) pl->tile_list.push_back(make_int4(i, mb, nb, 0));
+            for (int nb = 0; nb < p.n_pad / GBN; ++nb) pl->tile_list.push_back(make_int4(i, mb, nb, 0));
         pl->padded += 2.0 * p.S * (p.S + 1) / 2 * (double)p.m_pad * p.n_pad * p.k_pad;
     }
     std::vector<Item> all_items;
@@ -670,8 +729,7 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
     pl->ntiles = (int)pl->tile_list.size();
     CGB_CHECK(pl->tiles.reserve(std::max<size_t>(pl->tile_list.size(), 1) * sizeof(int4), st));
     pl->grid = std::max(1, std::min(pl->ntiles, num_sms()));
-    CGB_CHECK(pl->W.reserve((size_t)pl->grid * BM * BN * sizeof(ulonglong2), st));
-    CGB_CUDA(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    CGB_CUDA(cudaFuncSetAttribute(ozaki_grouped_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM));
     CGB_CHECK(upload_tiles(pl, 0, st));
     CGB_CHECK(capture(pl));
     // tuning replays the batch: only when that cannot change C (beta == 0 everywhere)
@@ -709,7 +767,7 @@ int oz_grouped_run(cosma_gpu_oz_grouped_plan* pl, cudaStream_t st) { return ozg:
 void oz_grouped_destroy(cosma_gpu_oz_grouped_plan* pl) { ozg::destroy(pl); }
 void oz_grouped_info(const cosma_gpu_oz_grouped_plan* pl, cosma_gpu_grouped_info* info) {
     info->tiles = pl->ntiles;
-    info->tile_policy = 3;  // 128 x 256 tensor-core tiles
+    info->tile_policy = 3;  // 128 x 64 tensor-core tiles, partial sums in TMEM
     info->dynamic_schedule = 0;
     info->warps_per_cta = oz::THREADS / 32;
     info->useful_flops = pl->useful;

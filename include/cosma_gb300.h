@@ -42,13 +42,15 @@ const char* cosma_gpu_last_error_string(void);
 const char* cosma_gpu_version(void);
 
 /* ------------------------------------------------------ arithmetic methods */
-/* NATIVE: FP64 (complex FP64) arithmetic on the FP64 tensor path.
+/* NATIVE: the operand type's own arithmetic on the FP64 pipe (the
+ *         reference's semantics).
  * OZAKI : FP64-accurate GEMM from integer slices (|digit| <= 16) multiplied
- *         exactly on the FP8 tensor cores with FP32 accumulation, recombined
- *         in FP64 (real double / complex double only).
+ *         exactly on the FP8 tensor cores, summed exactly in 128-bit integers
+ *         and rounded once (double and complex double).  On single-precision
+ *         data it selects BF16X3 (float) or NATIVE (complex float).
  * BF16X3: single precision from three BF16 slices per operand, six slice
  *         products accumulated in FP32 on the BF16 tensor cores (float only).
- * AUTO  : NATIVE for every type (the reference's semantics). */
+ * AUTO  : BF16X3 for float, NATIVE for the other types. */
 #define COSMA_GPU_METHOD_AUTO 0
 #define COSMA_GPU_METHOD_NATIVE 1
 #define COSMA_GPU_METHOD_OZAKI 2
