@@ -135,16 +135,16 @@ __device__ __forceinline__ uint32_t pack4_e4m3(int a, int b, int c, int e) {
 // Writes the S E4M3 digit slices of a (rows x k) operand, row-major with
 // row pitch k_pad, zero-padded to rows_pad x k_pad.  Each thread handles 16
 // consecutive K elements of one row.  kcontig: element (r, l) at X[l + r*ld],
-// else at X[r + l*ld].
+// else at X[r + l*ld].  A warp covers 8 rows x 64 K elements, so its slice
+// stores are 64-byte runs along K in either layout, and its loads are
+// 64-byte runs along rows (X[r + l*ld]) or along K (X[l + r*ld]).
 template <int S, bool KCONTIG>
 __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t k,
                                             const int* __restrict__ exps, int64_t k_pad, int64_t rows_pad,
                                             uint8_t* __restrict__ out, int64_t bx, int64_t by) {
     const int t = threadIdx.x;
-    int64_t r;
-    int kc;
-    if (KCONTIG) { r = bx * 64 + t / 4; kc = t % 4; }
-    else { r = bx * 64 + t % 64; kc = t / 64; }
+    const int64_t r = bx * 64 + t / 4;
+    const int kc = t % 4;
     const int64_t l0 = by * 64 + kc * 16;
     if (r >= rows_pad || l0 >= k_pad) return;
     const int E = r < rows ? exps[r] : 0;

@@ -179,19 +179,30 @@ constexpr int G_A = BM * BK, G_B = GBN * BK, G_STAGE = G_A + G_B;
 constexpr int G_SMEM = G_STAGES * G_STAGE + 1024 + 256;
 constexpr uint32_t G_WCOL = 2 * GBN;
 static_assert(G_WCOL + 4 * GBN <= 512, "TMEM columns");
+// Eight epilogue warps, two per TMEM lane quadrant, each draining 32 of the
+// tile's 64 columns: with short K the drains, not the MMAs, set the pace.
+constexpr int G_EPI_WARPS = 8;
+constexpr int G_THREADS = 64 + 32 * G_EPI_WARPS;
 
 // Drains the accumulator groups of one tile (rows mb*128.., columns
 // nb*64..) into the TMEM partial sums and, after the last group, rounds them
 // to FP64 and writes alpha*r + beta*C.
 template <class Release>
 __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc, int mb, int nb, uint32_t tmem,
-                                               int quad, int lane, uint64_t* accf, uint32_t& acc_it,
+                                               int quad, int half, int lane, uint64_t* accf, uint32_t& acc_it,
                                                uint64_t pol_stream, unsigned* err, Release release) {
     const int row = quad * 32 + lane;
     const int64_t gi = (int64_t)mb * BM + row;
     const int Ei = p.expA[gi];
     const uint32_t lanes = (uint32_t)(quad * 32) << 16;
     const int last = sc.n_groups - 1;
+    // output description in registers (the TMEM accesses clobber memory)
+    const int64_t m = p.m, n = p.n, ldc = p.ldc;
+    double* const C = p.C;
+    const int* const expB = p.expB;
+    const int L = p.L;
+    const double alpha = p.alpha, beta = p.beta;
+    const bool alpha_one = p.alpha_one, beta_zero = p.beta_zero;
     for (int g = 0; g <= last; ++g, ++acc_it) {
         const uint32_t buf = acc_it & 1;
         if (!__all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, err, kDevTimeoutAcc)))
@@ -199,7 +210,7 @@ __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc
         tc::tc_fence_after();
         const int sh = sc.gshift[g];
 #pragma unroll 1
-        for (int c = 0; c < GBN; c += 16) {
+        for (int c = half * (GBN / 2); c < (half + 1) * (GBN / 2); c += 16) {
             uint32_t v[16], w0[16], w1[16], w2[16], w3[16];
             tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c, v);
             if (g > 0) {
@@ -225,11 +236,11 @@ __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc
                     w3[j] = (uint32_t)(hi >> 32);
                 } else {
                     const int64_t gj = (int64_t)nb * GBN + c + j;
-                    if (gi < p.m && gj < p.n) {
-                        double r = i128_to_double(lo, hi, Ei + p.expB[gj] - p.L);
-                        double* cp = p.C + gi + gj * p.ldc;
-                        if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
-                        if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+                    if (gi < m && gj < n) {
+                        double r = i128_to_double(lo, hi, Ei + expB[gj] - L);
+                        double* cp = C + gi + gj * ldc;
+                        if (!alpha_one) r = __dmul_rn(alpha, r);
+                        if (!beta_zero) r = __dadd_rn(r, __dmul_rn(beta, *cp));
                         tc::st_f64_hint(cp, r, pol_stream);
                     }
                 }
@@ -254,7 +265,7 @@ __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc
 // problem's tensor maps (maps[2i], maps[2i+1] in global memory), schedule
 // and output description.  Tiles of problems that failed the check are
 // skipped by all three roles alike.
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(G_THREADS, 1)
     ozaki_grouped_gemm_kernel(const Prob* __restrict__ P, const CUtensorMap* __restrict__ maps,
                               const Schedule* __restrict__ scheds, const int4* __restrict__ tiles, int ntiles,
                               const int* __restrict__ okf, unsigned* err) {
@@ -275,7 +286,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&accf[b], 1);
-            tc::mbar_init(&acce[b], 128);
+            tc::mbar_init(&acce[b], 32 * G_EPI_WARPS);
         }
         tc::mbar_init(drain, 1);
         tc::fence_mbar_init();
@@ -292,18 +303,24 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int4 tl = tiles[t];
                 if (!okf[tl.x]) continue;
+                // the tile's parameters in registers: the waits below clobber
+                // memory, and reloading them from global memory on every K
+                // block would cost more than the MMAs of a short K block
                 const Prob& p = P[tl.x];
-                const Schedule& sc = scheds[p.sched];
+                const int kbc = p.kb_count, mpad = p.m_pad, npad = p.n_pad;
+                const Schedule* scp = scheds + p.sched;
+                const int ng = scp->n_groups;
                 const CUtensorMap* tmA = maps + 2 * tl.x;
                 const CUtensorMap* tmB = tmA + 1;
                 tc::prefetch_tmap(tmA);
                 tc::prefetch_tmap(tmB);
-                for (int g = 0; g < sc.n_groups && ok; ++g) {
-                    for (int kc = 0; kc < p.kb_count && ok; kc += KB_CHUNK) {
-                        const int kc1 = min(p.kb_count, kc + KB_CHUNK);
-                        for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
-                            const int arow = sc.us[u] * p.m_pad + tl.y * BM;
-                            const int brow = sc.ut[u] * p.n_pad + tl.z * GBN;
+                for (int g = 0; g < ng && ok; ++g) {
+                    const int u0 = scp->gfirst[g], u1 = u0 + scp->gcount[g];
+                    for (int kc = 0; kc < kbc && ok; kc += KB_CHUNK) {
+                        const int kc1 = min(kbc, kc + KB_CHUNK);
+                        for (int u = u0; u < u1 && ok; ++u) {
+                            const int arow = scp->us[u] * mpad + tl.y * BM;
+                            const int brow = scp->ut[u] * npad + tl.z * GBN;
                             for (int kb = kc; kb < kc1; ++kb, ++it) {
                                 const int st = it % G_STAGES;
                                 if (!tc::mbar_wait(&empty[st], ((it / G_STAGES) & 1) ^ 1, err, kDevTimeoutEmpty)) {
@@ -331,8 +348,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const int4 tl = tiles[t];
                 if (!okf[tl.x]) continue;
                 const Prob& p = P[tl.x];
-                const Schedule& sc = scheds[p.sched];
-                for (int g = 0; g < sc.n_groups && ok; ++g, ++acc_it) {
+                const int kbc = p.kb_count;
+                const Schedule* scp = scheds + p.sched;
+                const int ng = scp->n_groups;
+                for (int g = 0; g < ng && ok; ++g, ++acc_it) {
+                    const int u0 = scp->gfirst[g], u1 = u0 + scp->gcount[g];
                     const uint32_t buf = acc_it & 1;
                     if (!tc::mbar_wait(&acce[buf], ((acc_it >> 1) & 1) ^ 1, err, kDevTimeoutAccEmpty)) {
                         ok = false;
@@ -341,9 +361,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                     tc::tc_fence_after();
                     const uint32_t d_tmem = tmem + buf * GBN;
                     uint32_t accumulate = 0;
-                    for (int kc = 0; kc < p.kb_count && ok; kc += KB_CHUNK) {
-                        const int kc1 = min(p.kb_count, kc + KB_CHUNK);
-                        for (int u = sc.gfirst[g]; u < sc.gfirst[g] + sc.gcount[g] && ok; ++u) {
+                    for (int kc = 0; kc < kbc && ok; kc += KB_CHUNK) {
+                        const int kc1 = min(kbc, kc + KB_CHUNK);
+                        for (int u = u0; u < u1 && ok; ++u) {
                             for (int kb = kc; kb < kc1; ++kb, ++it) {
                                 const int st = it % G_STAGES;
                                 if (!tc::mbar_wait(&full[st], (it / G_STAGES) & 1, err, kDevTimeoutFull)) {
@@ -369,14 +389,15 @@ __global__ void __launch_bounds__(THREADS, 1)
             tc::mbar_wait_drain(drain, 0);
         }
     } else {  // ------------------------------------------------ epilogue
-        const int quad = warp & 3;
+        const int quad = warp & 3;         // TMEM lanes this warp may access
+        const int half = (warp - 2) / 4;  // which 32 of the 64 columns
         const uint64_t pol_stream = tc::policy_evict_first();
         uint32_t acc_it = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int4 tl = tiles[t];
             if (!okf[tl.x]) continue;
             const Prob& p = P[tl.x];
-            if (!gepilogue_tile(p, scheds[p.sched], tl.y, tl.z, tmem, quad, lane, accf, acc_it, pol_stream, err,
+            if (!gepilogue_tile(p, scheds[p.sched], tl.y, tl.z, tmem, quad, half, lane, accf, acc_it, pol_stream, err,
                                 [&](uint32_t buf) { tc::mbar_arrive(&acce[buf]); }))
                 break;
         }
@@ -461,7 +482,7 @@ int enqueue(Plan* pl, cudaStream_t st) {
         gsplit(sl.S, sl.kcontig, sl.count, P, (const Item*)pl->sitems.ptr + sl.first, (const int*)pl->ok.ptr, st);
     CGB_CUDA(cudaGetLastError());
     if (pl->ntiles) {
-        ozaki_grouped_gemm_kernel<<<pl->grid, THREADS, G_SMEM, st>>>(
+        ozaki_grouped_gemm_kernel<<<pl->grid, G_THREADS, G_SMEM, st>>>(
             P, (const CUtensorMap*)pl->maps.ptr, (const Schedule*)pl->scheds.ptr, (const int4*)pl->tiles.ptr,
             pl->ntiles, (const int*)pl->ok.ptr, (unsigned*)pl->err.ptr);
         CGB_CUDA(cudaGetLastError());
@@ -769,7 +790,7 @@ void oz_grouped_info(const cosma_gpu_oz_grouped_plan* pl, cosma_gpu_grouped_info
     info->tiles = pl->ntiles;
     info->tile_policy = 3;  // 128 x 64 tensor-core tiles, partial sums in TMEM
     info->dynamic_schedule = 0;
-    info->warps_per_cta = oz::THREADS / 32;
+    info->warps_per_cta = ozg::G_THREADS / 32;
     info->useful_flops = pl->useful;
     info->padded_flops = pl->padded;
     info->tuned_ms = pl->tuned_ms;
