@@ -46,7 +46,8 @@ def parse():
     p.add_argument("--phi", type=int, default=0)
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison run")
     p.add_argument("--no-variants", action="store_true", help="skip the phi = 8 / 32 variants")
-    p.add_argument("--config", default="precision", choices=["precision", "pdgemm", "sgemm", "grouped", "stream"],
+    p.add_argument("--config", default="precision",
+                   choices=["precision", "plain", "pdgemm", "sgemm", "grouped", "stream"],
                    help="precision: the headline line; pdgemm: the 1x1 ScaLAPACK configuration; "
                         "sgemm: the FP32 3xBF16 variant of the precision configuration; "
                         "grouped: the batching configuration")
@@ -489,6 +490,84 @@ def run_grouped(args):
     print(json.dumps(out), flush=True)
 
 
+def run_plain(args):
+    """The plain small configuration: DGEMM C = A*B, m = n = k = 2048, NN, alpha = 1,
+    beta = 0, A and B U[-1,1] from seeds 1 and 2.  The native FP64 drop-in on
+    device-resident data (value), the same call end to end through
+    cosma_gpu_local_multiply_d from host buffers (e2e, the one-rank
+    cosma::multiply), the error bound c*k*u*(|A||B|) against OpenBLAS on the
+    host, the Ozaki form beside it, and OpenBLAS itself timed on the host cores."""
+    import torch
+
+    import cosma_gb300 as cg
+    import oracle
+
+    n = 2048 if args.size == 16384 else args.size
+    dev = torch.device("cuda", 0)
+    A = oracle.uniform((n, n), 1)
+    B = oracle.uniform((n, n), 2)
+    dA = torch.from_numpy(A.reshape(-1, order="F")).to(dev)
+    dB = torch.from_numpy(B.reshape(-1, order="F")).to(dev)
+    dC = torch.empty(n * n, dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream(dev)
+    flops = 2.0 * n ** 3
+
+    def timed(method):
+        for _ in range(max(args.warmup, 3)):
+            cg.gemm_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, method=method, stream=s)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(args.steps):
+            cg.gemm_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, method=method, stream=s)
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, dC.cpu().numpy().reshape(n, n).T
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms, Cn = timed("native")
+    clocks = sampler.stop()
+    oms, Co = timed("ozaki")
+    # host reference (the reference's CPU arithmetic) and its timing
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        ref = A @ B
+        reps += 1
+        if time.perf_counter() - t0 > 10.0:
+            break
+    cpu_s = (time.perf_counter() - t0) / reps
+    absab = np.abs(A) @ np.abs(B)
+    bound = 2.0 * (n + 2) * 2.0 ** -53 * absab
+    within = bool(np.all(np.abs(Cn - ref) <= bound))
+    # end to end: cosma::local_multiply on a one-rank strategy, host buffers
+    hA = torch.from_numpy(A.reshape(-1, order="F")).pin_memory()
+    hB = torch.from_numpy(B.reshape(-1, order="F")).pin_memory()
+    hC = torch.empty(n * n, dtype=torch.float64).pin_memory()
+    cg.local_multiply(hA, hB, hC, n, n, n, 1.0, 0.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cg.local_multiply(hA, hB, hC, n, n, n, 1.0, 0.0)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    value = flops / (ms * 1e-3) / 1e12
+    out = {"metric": "plain FP64 DGEMM TFLOP/s (native drop-in)", "value": value, "unit": UNIT, "n_gpus": 1,
+           "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic U[-1,1], seeds 1 and 2",
+           "config": {"workload": f"plain: DGEMM NN m=n=k={n}, alpha=1, beta=0, column-major",
+                      "l2": "operands 32 MiB each, inside L2; dmma kernel re-reads tiles from L2"},
+           "within_ckuAB_bound": within, "bound": "2 (k+2) u (|A||B|) elementwise vs OpenBLAS",
+           "max_err_over_absab": float(np.max(np.abs(Cn - ref) / absab)),
+           "ozaki_form": {"tflops": flops / (oms * 1e-3) / 1e12, "ms": oms,
+                          "max_err_over_absab": float(np.max(np.abs(Co - ref) / absab))},
+           "e2e": {"value": flops / e2e_s / 1e12, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * n * n,
+                   "d2h_bytes_per_step": 8 * n * n, "entry": "cosma_gpu_local_multiply_d, pinned host buffers"},
+           "cpu_baseline": {"value": flops / cpu_s / 1e12, "unit": UNIT, "cores": oracle.openblas_threads(),
+                            "kind": "port", "sample": f"OpenBLAS DGEMM NN {n}^3, {reps} repetitions"},
+           "clocks": clocks, "gpu_launches": args.steps}
+    print(json.dumps(out), flush=True)
+
+
 def run_stream(args):
     """Out-of-HBM streaming through the Tiled-MM entry point from pinned host
     memory, with tile limits far below the problem so every operand streams:
@@ -641,6 +720,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "plain":
+        return run_plain(args)
     if args.config == "pdgemm":
         return run_pdgemm(args)
     if args.config == "grouped":

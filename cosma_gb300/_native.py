@@ -67,6 +67,7 @@ SIGNATURES = {
     "cosma_gpu_local_multiply_c": (i32, [vp, vp, vp, vp, i32, i32, i32, vp, vp, i32]),
     "cosma_gpu_local_multiply_z": (i32, [vp, vp, vp, vp, i32, i32, i32, vp, vp, i32]),
     "cosma_gpu_context_instance": (vp, [ch]),
+    "cosma_gpu_selftest_wait_timeout": (i32, [C.c_ulonglong, vp]),
     "cosma_gpu_dgemm_device": (i32, [i32, ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, vp]),
     "cosma_gpu_zgemm_device": (i32, [i32, ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "cosma_gpu_sgemm_device": (i32, [i32, ch, ch, i64, i64, i64, flt, vp, i64, vp, i64, flt, vp, i64, vp]),

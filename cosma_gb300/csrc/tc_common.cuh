@@ -47,15 +47,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Waits for the phase of `bar` with the given parity.  Returns false (after
 // recording `code` in *err unless another role already failed) when the wait
-// exceeds the limit or another role has reported an error.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* err, unsigned code) {
+// exceeds `limit_ns` or another role has reported an error.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* err, unsigned code,
+                                          unsigned long long limit_ns = kWaitLimitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     unsigned long long t0 = globaltimer();
     for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((i & 1023) == 0) {
             if (*(volatile unsigned*)err != 0) return false;
-            if (globaltimer() - t0 > kWaitLimitNs) {
+            if (globaltimer() - t0 > limit_ns) {
                 atomicCAS(err, 0u, code);
                 return false;
             }

@@ -40,6 +40,12 @@ int cosma_gpu_last_error(void);
 const char* cosma_gpu_last_error_string(void);
 /* Library version string. */
 const char* cosma_gpu_version(void);
+/* Exercises the failure path of the tensor-core pipelines: a kernel waits on
+ * a barrier nothing arrives on, through the bounded wait those pipelines use,
+ * for limit_ns (1 ms .. 2 s).  Returns COSMA_GPU_ERROR_DEVICE_TIMEOUT when the
+ * timeout was detected and reported (the expected outcome); the context stays
+ * usable.  No reference counterpart. */
+int cosma_gpu_selftest_wait_timeout(unsigned long long limit_ns, void* stream);
 
 /* ------------------------------------------------------ arithmetic methods */
 /* NATIVE: the operand type's own arithmetic on the FP64 pipe (the
