@@ -1,0 +1,136 @@
+// Host <-> HBM copies of column-major sub-matrices from pageable memory.
+//
+// A pageable cudaMemcpy goes through the driver's own small staging buffer
+// and one CPU thread; its speed varies widely between hosts (6.5 to 27 GB/s
+// measured on the same GB300 pool).  For pageable memory these copies stage
+// through two pinned buffers instead: host threads copy column blocks
+// into one buffer while the DMA engine moves the other, so the transfer runs
+// near the host link's pinned bandwidth.  Pinned (or registered) and device
+// memory take the direct cudaMemcpy2DAsync.
+#include "common.cuh"
+#include "runtime.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+namespace cgb {
+namespace {
+
+constexpr size_t kStageBytes = 128ull << 20;  // per staging buffer
+
+struct Stager {
+    void* buf[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    bool ok = false;
+};
+
+std::mutex g_stage_mu;
+Stager g_stager;  // one per process: the copies below hold g_stage_mu
+
+bool stager_ready() {
+    if (g_stager.ok) return true;
+    for (int i = 0; i < 2; ++i) {
+        if (cudaMallocHost(&g_stager.buf[i], kStageBytes) != cudaSuccess) { g_stager.buf[i] = nullptr; break; }
+        if (cudaEventCreateWithFlags(&g_stager.done[i], cudaEventDisableTiming) != cudaSuccess) break;
+    }
+    cudaGetLastError();
+    g_stager.ok = g_stager.buf[0] && g_stager.buf[1] && g_stager.done[0] && g_stager.done[1];
+    return g_stager.ok;
+}
+
+int copy_threads() {
+    static const int n = [] {
+        unsigned h = std::thread::hardware_concurrency();
+        return (int)std::max(1u, std::min(h ? h : 1u, 16u));
+    }();
+    return n;
+}
+
+// Copies `cols` columns of `width` bytes between pitched layouts on `nt` threads.
+void parallel_copy(char* dst, size_t dpitch, const char* src, size_t spitch, size_t width, size_t cols) {
+    const size_t bytes = width * cols;
+    const int nt = bytes < (8u << 20) ? 1 : copy_threads();
+    auto work = [&](int t) {
+        const size_t c0 = cols * t / nt, c1 = cols * (t + 1) / nt;
+        if (dpitch == width && spitch == width) {
+            std::memcpy(dst + c0 * width, src + c0 * width, (c1 - c0) * width);
+        } else {
+            for (size_t c = c0; c < c1; ++c) std::memcpy(dst + c * dpitch, src + c * spitch, width);
+        }
+    };
+    if (nt == 1) {
+        work(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+}
+
+bool pageable(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return at.type == cudaMemoryTypeUnregistered;
+}
+
+}  // namespace
+
+int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                cudaStream_t s) {
+    if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    std::lock_guard<std::mutex> lock(g_stage_mu);
+    if (!pageable(src) || width > kStageBytes || !stager_ready()) {
+        CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, s));
+        return COSMA_GPU_SUCCESS;
+    }
+    const size_t per = kStageBytes / width;  // columns per staging buffer
+    int b = 0;
+    for (size_t c0 = 0; c0 < cols; c0 += per, b ^= 1) {
+        const size_t nc = std::min(per, cols - c0);
+        CGB_CUDA(cudaEventSynchronize(g_stager.done[b]));  // the DMA out of this buffer has finished
+        parallel_copy((char*)g_stager.buf[b], width, (const char*)src + c0 * spitch, spitch, width, nc);
+        CGB_CUDA(cudaMemcpy2DAsync((char*)dst + c0 * dpitch, dpitch, g_stager.buf[b], width, width, nc,
+                                   cudaMemcpyHostToDevice, s));
+        CGB_CUDA(cudaEventRecord(g_stager.done[b], s));
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                cudaStream_t s) {
+    if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    std::lock_guard<std::mutex> lock(g_stage_mu);
+    if (!pageable(dst) || width > kStageBytes || !stager_ready()) {
+        CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, cudaMemcpyDeviceToHost, s));
+        CGB_CUDA(cudaStreamSynchronize(s));
+        return COSMA_GPU_SUCCESS;
+    }
+    const size_t per = kStageBytes / width;
+    const size_t nchunks = (cols + per - 1) / per;
+    // DMA of chunk i+1 overlaps the host copy of chunk i out of the other buffer
+    auto issue = [&](size_t i) -> int {
+        const size_t c0 = i * per, nc = std::min(per, cols - c0);
+        CGB_CUDA(cudaMemcpy2DAsync(g_stager.buf[i & 1], width, (const char*)src + c0 * spitch, spitch, width, nc,
+                                   cudaMemcpyDeviceToHost, s));
+        CGB_CUDA(cudaEventRecord(g_stager.done[i & 1], s));
+        return COSMA_GPU_SUCCESS;
+    };
+    CGB_CHECK(issue(0));
+    for (size_t i = 0; i < nchunks; ++i) {
+        if (i + 1 < nchunks) CGB_CHECK(issue(i + 1));
+        CGB_CUDA(cudaEventSynchronize(g_stager.done[i & 1]));
+        const size_t c0 = i * per, nc = std::min(per, cols - c0);
+        parallel_copy((char*)dst + c0 * dpitch, dpitch, (const char*)g_stager.buf[i & 1], width, width, nc);
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace cgb

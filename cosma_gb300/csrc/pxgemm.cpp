@@ -94,8 +94,7 @@ int stage_in(const void* p, int64_t rows, int64_t cols, int64_t ld, size_t es, D
     *dptr = buf.ptr;
     *dld = std::max<int64_t>(rows, 1);
     if (copy && rows > 0 && cols > 0)
-        CGB_CUDA(cudaMemcpy2DAsync(buf.ptr, (size_t)*dld * es, p, (size_t)ld * es, (size_t)rows * es, (size_t)cols,
-                                   cudaMemcpyHostToDevice, s));
+        CGB_CHECK(copy_h2d_2d(buf.ptr, (size_t)*dld * es, p, (size_t)ld * es, (size_t)rows * es, (size_t)cols, s));
     return COSMA_GPU_SUCCESS;
 }
 
@@ -132,8 +131,7 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
         int64_t ldC;
         CGB_CHECK(stage_in(csub, m, n, lldc, es, g_px_buf[5], !beta_zero, &dC, &ldC, s));
         CGB_CHECK(scale_matrix_device(sc, m, n, beta, (void*)dC, ldC, s));
-        if (!c_dev)
-            CGB_CUDA(cudaMemcpy2DAsync(csub, lldc * es, dC, ldC * es, (size_t)m * es, n, cudaMemcpyDeviceToHost, s));
+        if (!c_dev) CGB_CHECK(copy_d2h_2d(csub, lldc * es, dC, ldC * es, (size_t)m * es, n, s));
         CGB_CUDA(cudaStreamSynchronize(s));
         return COSMA_GPU_SUCCESS;
     }
@@ -172,8 +170,7 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
     CGB_CHECK(gemm_device(g, px_method(), 0, s, nullptr));
     // 4. C_sc = alpha * C_cosma + beta * C_sc
     CGB_CHECK(unpack_device(sc, m, n, alpha, dCc, m, beta, (void*)dCsc, ldCsc, s));
-    if (!c_dev)
-        CGB_CUDA(cudaMemcpy2DAsync(csub, lldc * es, dCsc, ldCsc * es, (size_t)m * es, n, cudaMemcpyDeviceToHost, s));
+    if (!c_dev) CGB_CHECK(copy_d2h_2d(csub, lldc * es, dCsc, ldCsc * es, (size_t)m * es, n, s));
     CGB_CUDA(cudaStreamSynchronize(s));
     return COSMA_GPU_SUCCESS;
 }

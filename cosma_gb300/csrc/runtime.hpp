@@ -76,6 +76,15 @@ int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, co
                   const double* beta, void* dst, int64_t ldd, cudaStream_t s);  // layout.cu
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
 
+// Column-major sub-matrix copies between host and HBM (host_copy.cpp):
+// pageable host memory goes through pinned staging buffers filled by
+// several host threads; pinned / device memory is copied directly.  The D2H
+// form returns once the data is in host memory.
+int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                cudaStream_t s);
+int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                cudaStream_t s);
+
 // Grouped Ozaki-split FP64 GEMM (ozaki_grouped.cu), driven by the grouped
 // plan of grouped.cu when it is created with the Ozaki method.
 cosma_gpu_oz_grouped_plan* oz_grouped_create(int count, const cosma_gpu_gemm_problem* problems, int autotune,

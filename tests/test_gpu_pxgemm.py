@@ -120,3 +120,28 @@ def test_psgemm(native_lib, cuda):
     # FP32: validate_results 1e-6 relative to max(1e-3, |v|) at k = 40
     _run_case(30, 40, 40, 20, 30, 20, 8, 8, 8, 8, 8, 8, 1, 1, 1, 1, 1, 1, 30, 20, 40, "N", "N", 1.0, 0.0, 30, 40, 30,
               dtype=np.float32)
+
+
+def test_large_host_arrays_through_staged_copies(native_lib, cuda):
+    """Host (pageable) operands larger than one pinned staging buffer
+    (128 MiB) travel in several chunks; the result must be bit-identical to
+    the same pdgemm on device arrays, and C outside the sub-matrix untouched."""
+    import torch
+    from cosma_gb300 import descinit, pxgemm
+    m, n, k = 1500, 1300, 12000            # A^T: 12000 x 1500 x 8 B = 144 MB, B: 125 MB
+    lda, ldb, ldc = k + 3, k, m + 5
+    A = oracle.uniform((lda, m), 11)
+    B = oracle.uniform((ldb, n), 12)
+    C = oracle.uniform((ldc, n + 2), 13)
+    desca = descinit(k, m, 128, 128, 0, 0, 0, lda)
+    descb = descinit(k, n, 128, 128, 0, 0, 0, ldb)
+    descc = descinit(m, n + 2, 128, 128, 0, 0, 0, ldc)
+    dA = torch.from_numpy(A.reshape(-1, order="F").copy()).cuda()
+    dB = torch.from_numpy(B.reshape(-1, order="F").copy()).cuda()
+    dC = torch.from_numpy(C.reshape(-1, order="F").copy()).cuda()
+    pxgemm("T", "N", m, n, k, 1.5, dA, 1, 1, desca, dB, 1, 1, descb, 0.5, dC, 1, 2, descc, scalar="d")
+    Ch = C.copy(order="F")
+    pxgemm("T", "N", m, n, k, 1.5, A, 1, 1, desca, B, 1, 1, descb, 0.5, Ch, 1, 2, descc)
+    dev = dC.cpu().numpy().reshape(n + 2, ldc).T
+    assert Ch.tobytes() == np.asfortranarray(dev).tobytes()
+    assert Ch[:, 0].tobytes() == C[:, 0].tobytes()   # column outside jc..jc+n-1
