@@ -174,8 +174,14 @@ __global__ void __launch_bounds__(256) gsplit_kernel(const Prob* __restrict__ P,
 // so a drain never leaves the SM.  The B slab of a stage shrinks to 8 KB, and
 // eight 24 KB stages fit in shared memory.
 constexpr int GBN = 64;
-constexpr int G_STAGES = 8;
-constexpr int G_A = BM * BK, G_B = GBN * BK, G_STAGE = G_A + G_B;
+// A stage carries two consecutive 128-byte K blocks of one slice product (8
+// MMAs of 128 x 64 x 32): the wait / commit round trip of a stage costs ~300
+// cycles that the MMAs of the stage must cover, and 4 MMAs of N = 64 (48
+// cycles each) do not.  Layout of a stage: A block 0 | A block 1 | B block 0 |
+// B block 1, every part 1024-byte aligned.
+constexpr int G_STAGES = 4;
+constexpr int G_KB_PER_STAGE = 2;
+constexpr int G_A = BM * BK, G_B = GBN * BK, G_STAGE = G_KB_PER_STAGE * (G_A + G_B);
 constexpr int G_SMEM = G_STAGES * G_STAGE + 1024 + 256;
 constexpr uint32_t G_WCOL = 2 * GBN;
 static_assert(G_WCOL + 4 * GBN <= 512, "TMEM columns");
@@ -321,16 +327,20 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                         for (int u = u0; u < u1 && ok; ++u) {
                             const int arow = scp->us[u] * mpad + tl.y * BM;
                             const int brow = scp->ut[u] * npad + tl.z * GBN;
-                            for (int kb = kc; kb < kc1; ++kb, ++it) {
+                            for (int kb = kc; kb < kc1; kb += G_KB_PER_STAGE, ++it) {
                                 const int st = it % G_STAGES;
+                                const int nkb = min(G_KB_PER_STAGE, kc1 - kb);
                                 if (!tc::mbar_wait(&empty[st], ((it / G_STAGES) & 1) ^ 1, err, kDevTimeoutEmpty)) {
                                     ok = false;
                                     break;
                                 }
-                                tc::mbar_arrive_expect_tx(&full[st], G_STAGE);
+                                tc::mbar_arrive_expect_tx(&full[st], nkb * (G_A + G_B));
                                 uint8_t* sa = smem + st * G_STAGE;
-                                tc::tma_load_2d(sa, tmA, kb * BK, arow, &full[st]);
-                                tc::tma_load_2d(sa + G_A, tmB, kb * BK, brow, &full[st]);
+                                for (int j = 0; j < nkb; ++j) {
+                                    tc::tma_load_2d(sa + j * G_A, tmA, (kb + j) * BK, arow, &full[st]);
+                                    tc::tma_load_2d(sa + G_KB_PER_STAGE * G_A + j * G_B, tmB, (kb + j) * BK, brow,
+                                                    &full[st]);
+                                }
                             }
                         }
                     }
@@ -364,19 +374,23 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                     for (int kc = 0; kc < kbc && ok; kc += KB_CHUNK) {
                         const int kc1 = min(kbc, kc + KB_CHUNK);
                         for (int u = u0; u < u1 && ok; ++u) {
-                            for (int kb = kc; kb < kc1; ++kb, ++it) {
+                            for (int kb = kc; kb < kc1; kb += G_KB_PER_STAGE, ++it) {
                                 const int st = it % G_STAGES;
+                                const int nkb = min(G_KB_PER_STAGE, kc1 - kb);
                                 if (!tc::mbar_wait(&full[st], (it / G_STAGES) & 1, err, kDevTimeoutFull)) {
                                     ok = false;
                                     break;
                                 }
                                 tc::tc_fence_after();
                                 const uint32_t sa = tc::smem_u32(smem + st * G_STAGE);
-                                const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + G_A);
+                                for (int j = 0; j < nkb; ++j) {
+                                    const uint64_t ad = tc::sdesc_k_sw128(sa + j * G_A);
+                                    const uint64_t bd = tc::sdesc_k_sw128(sa + G_KB_PER_STAGE * G_A + j * G_B);
 #pragma unroll
-                                for (int kk = 0; kk < BK / 32; ++kk) {
-                                    tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
-                                    accumulate = 1;
+                                    for (int kk = 0; kk < BK / 32; ++kk) {
+                                        tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
+                                        accumulate = 1;
+                                    }
                                 }
                                 tc::mma_commit(&empty[st]);
                             }
