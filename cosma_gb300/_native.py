@@ -45,6 +45,16 @@ class GroupedInfo(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class Block(C.Structure):  # cosma_gpu_block (the reference's `block`)
+    _fields_ = [("data", C.c_void_p), ("ld", C.c_int), ("row", C.c_int), ("col", C.c_int)]
+
+
+class Layout(C.Structure):  # cosma_gpu_layout (the reference's `layout`)
+    _fields_ = [("rowblocks", C.c_int), ("colblocks", C.c_int), ("rowsplit", C.POINTER(C.c_int)),
+                ("colsplit", C.POINTER(C.c_int)), ("owners", C.POINTER(C.c_int)), ("nlocalblocks", C.c_int),
+                ("localblocks", C.POINTER(Block))]
+
+
 i32, i64, dbl, flt, vp, ch = C.c_int, C.c_int64, C.c_double, C.c_float, C.c_void_p, C.c_char
 _PX = [vp] * 19
 
@@ -68,6 +78,14 @@ SIGNATURES = {
     "cosma_gpu_local_multiply_z": (i32, [vp, vp, vp, vp, i32, i32, i32, vp, vp, i32]),
     "cosma_gpu_context_instance": (vp, [ch]),
     "cosma_gpu_selftest_wait_timeout": (i32, [C.c_ulonglong, vp]),
+    "cosma_gpu_smultiply_using_layout": (i32, [C.c_char_p, C.c_char_p, vp, C.POINTER(Layout), C.POINTER(Layout), vp,
+                                               C.POINTER(Layout)]),
+    "cosma_gpu_dmultiply_using_layout": (i32, [C.c_char_p, C.c_char_p, vp, C.POINTER(Layout), C.POINTER(Layout), vp,
+                                               C.POINTER(Layout)]),
+    "cosma_gpu_cmultiply_using_layout": (i32, [C.c_char_p, C.c_char_p, vp, C.POINTER(Layout), C.POINTER(Layout), vp,
+                                               C.POINTER(Layout)]),
+    "cosma_gpu_zmultiply_using_layout": (i32, [C.c_char_p, C.c_char_p, vp, C.POINTER(Layout), C.POINTER(Layout), vp,
+                                               C.POINTER(Layout)]),
     "cosma_gpu_dgemm_device": (i32, [i32, ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, vp]),
     "cosma_gpu_zgemm_device": (i32, [i32, ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "cosma_gpu_sgemm_device": (i32, [i32, ch, ch, i64, i64, i64, flt, vp, i64, vp, i64, flt, vp, i64, vp]),

@@ -214,6 +214,38 @@ def zgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm,
     return info.as_dict()
 
 
+class BlockLayout:
+    """A matrix described block by block, as the reference's C `layout`:
+    block (r, c) covers rows rowsplit[r]:rowsplit[r+1] and columns
+    colsplit[c]:colsplit[c+1]; `blocks[(r, c)] = (buffer, ld)` with a
+    column-major host array or CUDA tensor.  All blocks belong to rank 0."""
+
+    def __init__(self, rowsplit, colsplit, blocks, owners=None):
+        self.rowsplit = (C.c_int * len(rowsplit))(*rowsplit)
+        self.colsplit = (C.c_int * len(colsplit))(*colsplit)
+        nb = (len(rowsplit) - 1) * (len(colsplit) - 1)
+        self.owners = (C.c_int * max(1, nb))(*(owners or [0] * nb))
+        items = list(blocks.items())
+        self.blocks = (N.Block * max(1, len(items)))()
+        for i, ((r, c), (buf, ld)) in enumerate(items):
+            self.blocks[i] = N.Block(ptr(buf), int(ld), int(r), int(c))
+        self._keep = blocks
+        self.c = N.Layout(len(rowsplit) - 1, len(colsplit) - 1, self.rowsplit, self.colsplit, self.owners,
+                          len(items), self.blocks)
+
+
+def multiply_using_layout(transa, transb, alpha, a: BlockLayout, b: BlockLayout, beta, c: BlockLayout, scalar="d"):
+    """cosma::multiply_using_layout on one rank (the reference's C interface):
+    C = alpha * op(A) * op(B) + beta * C over block layouts."""
+    lib = N.load()
+    rt = C.c_double if scalar in "dz" else C.c_float
+    al = (rt * 1)(alpha) if scalar in "sd" else _cplx_pair(alpha, rt)
+    be = (rt * 1)(beta) if scalar in "sd" else _cplx_pair(beta, rt)
+    f = getattr(lib, f"cosma_gpu_{scalar}multiply_using_layout")
+    N.check(f(transa.encode(), transb.encode(), C.cast(al, C.c_void_p), C.byref(a.c), C.byref(b.c),
+              C.cast(be, C.c_void_p), C.byref(c.c)))
+
+
 class GroupedPlan:
     """A grouped FP64 GEMM over many device problems, one persistent launch
     replayed from a CUDA graph (method "native" or "ozaki").  `problems` is a list of tuples

@@ -27,9 +27,6 @@
 extern "C" void Cblacs_gridinfo(int ctxt, int* nprow, int* npcol, int* myrow, int* mycol) __attribute__((weak));
 
 namespace cgb {
-GemmDesc make_gemm_desc(Scalar s, char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,
-                        const void* A, int64_t lda, const void* B, int64_t ldb, const double* beta, void* C,
-                        int64_t ldc);
 int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t cols, const void* src, int64_t lds,
                 void* dst, int64_t ldd, cudaStream_t s);
 int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
@@ -176,6 +173,12 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
 }
 
 }  // namespace
+
+int process_gemm_method() {
+    std::lock_guard<std::mutex> lock(g_px_mu);
+    return px_method();
+}
+
 }  // namespace cgb
 
 // The ScaLAPACK entry points are void (as in the reference); their status is

@@ -76,6 +76,10 @@ int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, co
                   const double* beta, void* dst, int64_t ldd, cudaStream_t s);  // layout.cu
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
 
+// The method of the process-wide entry points (p?gemm, multiply_using_layout):
+// cosma_gpu_pxgemm_set_method, else COSMA_GPU_GEMM_METHOD (pxgemm.cpp).
+int process_gemm_method();
+
 // Column-major sub-matrix copies between host and HBM (host_copy.cpp):
 // pageable host memory goes through pinned staging buffers filled by
 // several host threads; pinned / device memory is copied directly.  The D2H
@@ -96,6 +100,9 @@ int oz_grouped_slices(const cosma_gpu_oz_grouped_plan* pl, int* out);
 
 // Dispatches one device-pointer GEMM by method (handles the k == 0 /
 // alpha == 0 corner cases).  Defined in gemm_dispatch.cpp.
+GemmDesc make_gemm_desc(Scalar s, char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,
+                        const void* A, int64_t lda, const void* B, int64_t ldb, const double* beta, void* C,
+                        int64_t ldc);  // gemm_dispatch.cpp
 int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t stream,
                 cosma_gpu_ozaki_info* info);
 

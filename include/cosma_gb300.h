@@ -253,6 +253,48 @@ void cosma_gpu_grouped_plan_destroy(cosma_gpu_grouped_plan* plan);
 int cosma_gpu_dgemm_grouped_device(int method, int count, const cosma_gpu_gemm_problem* problems,
                                    void* stream);
 
+/* ------------------------------------------- multiply_using_layout (C API) */
+/* Replaces the reference's C interface for arbitrary block layouts
+ * (src/cosma/cinterface.hpp:9-40, cinterface.cpp:55-147; multiply.cpp:78-213)
+ * on one rank.  The two structs have the reference's `block` / `layout`
+ * memory layout, so existing descriptions can be passed by pointer.
+ *   rowsplit[rowblocks + 1], colsplit[colblocks + 1]: block boundaries;
+ *   owners[rowblocks * colblocks]: must all be 0 (one rank);
+ *   localblocks[nlocalblocks]: every block (row, col) exactly once, column-major
+ *   with leading dimension ld, in host or device memory.
+ * The layouts describe the matrices as stored: op(A) is m x k, so A is m x k
+ * for 'N' and k x m for 'T' / 'C' (the reference derives m and k from the
+ * stored shape, which coincide for 'N').  Computes
+ * C = alpha * op(A) * op(B) + beta * C with the process-wide method
+ * (cosma_gpu_pxgemm_set_method / COSMA_GPU_GEMM_METHOD). */
+typedef struct cosma_gpu_block {
+    void* data;
+    const int ld;
+    const int row;
+    const int col;
+} cosma_gpu_block;
+typedef struct cosma_gpu_layout {
+    int rowblocks;
+    int colblocks;
+    const int* rowsplit;
+    const int* colsplit;
+    const int* owners;
+    int nlocalblocks;
+    cosma_gpu_block* localblocks;
+} cosma_gpu_layout;
+int cosma_gpu_smultiply_using_layout(const char* transa, const char* transb, const float* alpha,
+                                     const cosma_gpu_layout* a, const cosma_gpu_layout* b,
+                                     const float* beta, const cosma_gpu_layout* c);
+int cosma_gpu_dmultiply_using_layout(const char* transa, const char* transb, const double* alpha,
+                                     const cosma_gpu_layout* a, const cosma_gpu_layout* b,
+                                     const double* beta, const cosma_gpu_layout* c);
+int cosma_gpu_cmultiply_using_layout(const char* transa, const char* transb, const float* alpha,
+                                     const cosma_gpu_layout* a, const cosma_gpu_layout* b,
+                                     const float* beta, const cosma_gpu_layout* c);
+int cosma_gpu_zmultiply_using_layout(const char* transa, const char* transb, const double* alpha,
+                                     const cosma_gpu_layout* a, const cosma_gpu_layout* b,
+                                     const double* beta, const cosma_gpu_layout* c);
+
 /* ------------------------------------- COSTA 1x1-grid layout transforms */
 /* dst(rows x cols) = op(src) where op in {'N','T','C'}: the block-cyclic ->
  * COSMA-blocked pack that costa::transformer::schedule(scalapack -> cosma,
