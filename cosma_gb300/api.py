@@ -78,6 +78,15 @@ class MMHandle:
         N.check(self.lib.cosma_gpu_tmm_last_ozaki_info(self._h, C.byref(info)))
         return info.as_dict()
 
+    def set_memory_limit(self, nbytes):
+        """Square tiles whose device footprint fits in nbytes (see tiles_for_memory)."""
+        N.check(self.lib.cosma_gpu_tmm_set_memory_limit(self._h, int(nbytes)))
+
+    def tiles(self):
+        t = [C.c_int(), C.c_int(), C.c_int()]
+        N.check(self.lib.cosma_gpu_tmm_tiles(self._h, *(C.byref(x) for x in t)))
+        return tuple(x.value for x in t)
+
     def transfer_bytes(self):
         """(host->device, device->host) bytes moved by the last gemm call."""
         h2d, d2h = C.c_int64(), C.c_int64()
@@ -97,6 +106,15 @@ class MMHandle:
             self.close()
         except Exception:
             pass
+
+
+def tiles_for_memory(scalar, method, nbytes):
+    """Largest square tiles (multiple of 256) whose handle footprint fits in nbytes."""
+    lib = N.load()
+    t = [C.c_int(), C.c_int(), C.c_int()]
+    meth = N.METHODS[method] if isinstance(method, str) else int(method)
+    N.check(lib.cosma_gpu_tmm_tiles_for_memory(scalar.encode(), meth, int(nbytes), *(C.byref(x) for x in t)))
+    return tuple(x.value for x in t)
 
 
 def make_context(scalar="d", streams=0, tile_m=0, tile_n=0, tile_k=0) -> MMHandle:

@@ -29,12 +29,6 @@
 #include <mutex>
 #include <vector>
 
-namespace cgb {
-GemmDesc make_gemm_desc(Scalar s, char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,
-                        const void* A, int64_t lda, const void* B, int64_t ldb, const double* beta, void* C,
-                        int64_t ldc);
-}
-
 struct cosma_gpu_mm_handle {
     cgb::Scalar scalar = cgb::Scalar::D;
     int n_streams = 3, tile_m = 0, tile_n = 0, tile_k = 0;
@@ -432,6 +426,69 @@ int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* h, int method, int slices) {
     std::lock_guard<std::mutex> lock(h->mu);
     h->method = method;
     h->slices = slices;
+    return COSMA_GPU_SUCCESS;
+}
+
+// Device bytes a handle needs at square tiles of edge t: the double-buffered
+// A, B and C tile slots, plus the method's scratch at its worst case (16
+// digit slices per operand and the per-CTA partial sums for the Ozaki form,
+// three BF16 slices for 3xBF16).
+static double tmm_footprint(cgb::Scalar s, int method, double t) {
+    const double es = (double)cgb::scalar_bytes(s);
+    double bytes = 2.0 * 3.0 * t * t * es;
+    if (method == COSMA_GPU_METHOD_AUTO) method = s == cgb::Scalar::S ? COSMA_GPU_METHOD_BF16X3 : COSMA_GPU_METHOD_NATIVE;
+    if (method == COSMA_GPU_METHOD_OZAKI && s == cgb::Scalar::S) method = COSMA_GPU_METHOD_BF16X3;
+    if (method == COSMA_GPU_METHOD_OZAKI && s == cgb::Scalar::D)
+        bytes += 16.0 * 2.0 * t * t + 152.0 * 128 * 256 * 16;
+    if (method == COSMA_GPU_METHOD_OZAKI && s == cgb::Scalar::Z)
+        bytes += 16.0 * 6.0 * t * t + 152.0 * 128 * 256 * 16 + 16.0 * t * t;
+    if (method == COSMA_GPU_METHOD_BF16X3 && s == cgb::Scalar::S) bytes += 3.0 * 2.0 * 2.0 * t * t;
+    return bytes;
+}
+
+// The largest square tile edge (a multiple of 256) whose handle footprint
+// fits in `bytes`: the one-GPU counterpart of COSMA's sequential splits
+// under a memory limit (src/cosma/strategy.cpp:404-440), which cut a problem
+// into steps that fit the memory; here the tile streamer runs the steps.
+int cosma_gpu_tmm_tiles_for_memory(char scalar, int method, int64_t bytes, int* tile_m, int* tile_n, int* tile_k) {
+    cgb::clear_error();
+    cgb::Scalar s;
+    if (!parse_scalar(scalar, &s) || !tile_m || !tile_n || !tile_k)
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "tiles_for_memory: bad argument");
+    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_BF16X3)
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "tiles_for_memory: unknown method");
+    int64_t best = 0;
+    for (int64_t t = 256; t <= (1 << 20); t += 256) {
+        if (tmm_footprint(s, method, (double)t) > (double)bytes) break;
+        best = t;
+    }
+    if (!best)
+        return cgb::set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY,
+                              "tiles_for_memory: not even 256 x 256 tiles fit in " + std::to_string(bytes) + " bytes");
+    *tile_m = *tile_n = *tile_k = (int)std::min<int64_t>(best, 1 << 30);
+    return COSMA_GPU_SUCCESS;
+}
+
+int cosma_gpu_tmm_set_memory_limit(cosma_gpu_mm_handle* h, int64_t bytes) {
+    cgb::clear_error();
+    if (!h) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "set_memory_limit: null handle");
+    std::lock_guard<std::mutex> lock(h->mu);
+    const char sc = h->scalar == cgb::Scalar::S ? 's' : h->scalar == cgb::Scalar::D ? 'd'
+                  : h->scalar == cgb::Scalar::C ? 'c' : 'z';
+    int tm = 0, tn = 0, tk = 0;
+    CGB_CHECK(cosma_gpu_tmm_tiles_for_memory(sc, h->method, bytes, &tm, &tn, &tk));
+    h->tile_m = tm;
+    h->tile_n = tn;
+    h->tile_k = tk;
+    return COSMA_GPU_SUCCESS;
+}
+
+int cosma_gpu_tmm_tiles(cosma_gpu_mm_handle* h, int* tile_m, int* tile_n, int* tile_k) {
+    if (!h || !tile_m || !tile_n || !tile_k) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "tiles: null");
+    std::lock_guard<std::mutex> lock(h->mu);
+    *tile_m = h->tile_m;
+    *tile_n = h->tile_n;
+    *tile_k = h->tile_k;
     return COSMA_GPU_SUCCESS;
 }
 

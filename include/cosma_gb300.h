@@ -95,6 +95,17 @@ int cosma_gpu_tmm_last_transfer_bytes(cosma_gpu_mm_handle* handle, int64_t* h2d_
                                       int64_t* d2h_bytes);
 /* Ozaki statistics of the handle's last call. */
 int cosma_gpu_tmm_last_ozaki_info(cosma_gpu_mm_handle* handle, cosma_gpu_ozaki_info* info);
+/* Memory limit: the largest square tiles (multiple of 256) whose device
+ * footprint (double-buffered A, B, C tile slots plus the method's worst-case
+ * scratch) fits in `bytes`; the one-GPU counterpart of COSMA's sequential
+ * splits under a memory limit (src/cosma/strategy.cpp:404-440).  The streamer
+ * then runs problems of any size in steps of these tiles.
+ * tiles_for_memory computes the tiles only; set_memory_limit applies them to
+ * a handle (for its current method); tiles reads them back. */
+int cosma_gpu_tmm_tiles_for_memory(char scalar, int method, int64_t bytes, int* tile_m, int* tile_n,
+                                   int* tile_k);
+int cosma_gpu_tmm_set_memory_limit(cosma_gpu_mm_handle* handle, int64_t bytes);
+int cosma_gpu_tmm_tiles(cosma_gpu_mm_handle* handle, int* tile_m, int* tile_n, int* tile_k);
 
 /* Replaces gpu::gemm(mm_handle<T>&, transa, transb, m, n, k, alpha, A, lda,
  * B, ldb, beta, C, ldc, pin_host_buffers, copy_c_back)

@@ -163,3 +163,25 @@ def test_tiled_mm_handle_with_ozaki_method(native_lib, cuda):
     assert st["max_err_over_absab"] <= 2.0 ** -51  # K tiles add one rounding each
     assert h.ozaki_info()["slices"] == 13
     h.close()
+
+
+def test_memory_limited_handle_streams_in_tiles(native_lib, cuda):
+    """A handle under a 256 MiB device budget runs a larger Ozaki DGEMM from
+    host memory in tiles: the operands travel several times and the result
+    still meets the accuracy bound."""
+    from cosma_gb300 import gemm, make_context
+    h = make_context("d", 2, 0, 0, 0)
+    h.set_method("ozaki", 0)
+    h.set_memory_limit(256 << 20)
+    tm, tn, tk = h.tiles()
+    m, n, k = 3000, 2600, 2800
+    assert tm < m and tk < k
+    A, B = oracle.uniform((m, k), 31), oracle.uniform((k, n), 32)
+    Cg = np.zeros((m, n), order="F")
+    gemm(h, "N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cg, m)
+    h2d, d2h = h.transfer_bytes()
+    assert h2d > (A.nbytes + B.nbytes)  # operand tiles are re-sent across output tiles
+    rng = np.random.default_rng(3)
+    rows, cols = rng.integers(0, m, 512), rng.integers(0, n, 512)
+    hi, lo, ab = oracle.gemm_dd_sampled("N", "N", A, B, rows, cols)
+    assert oracle.error_stats(Cg[rows, cols], hi, lo, ab)["max_err_over_absab"] <= 2.0 ** -51

@@ -39,3 +39,23 @@ def test_rejects_malformed_layouts(native_lib):
         with pytest.raises(CosmaGpuError) as e:
             multiply_using_layout("N", "N", 1.0, a, b, 0.0, c)
         assert e.value.code == code, e.value
+
+
+def test_tiles_for_memory_fit_and_grow(native_lib):
+    """The memory-limited tiling (sequential-split counterpart): tiles are
+    multiples of 256, grow with the budget, shrink for methods with more
+    scratch, and an impossible budget is an OUT_OF_MEMORY error."""
+    from cosma_gb300 import CosmaGpuError, tiles_for_memory
+    budgets = [2 ** 28, 2 ** 30, 2 ** 33, 2 ** 36]
+    for scalar in "sdcz":
+        for method in ("native", "ozaki", "bf16x3", "auto"):
+            t = [tiles_for_memory(scalar, method, b)[0] for b in budgets]
+            assert all(x % 256 == 0 and x > 0 for x in t)
+            assert t == sorted(t)
+            es = {"s": 4, "d": 8, "c": 8, "z": 16}[scalar]
+            for x, b in zip(t, budgets):
+                assert 6 * x * x * es <= b  # the A, B, C tile slots alone fit
+    assert tiles_for_memory("d", "ozaki", 2 ** 30)[0] < tiles_for_memory("d", "native", 2 ** 30)[0]
+    with pytest.raises(CosmaGpuError) as e:
+        tiles_for_memory("d", "native", 1 << 20)
+    assert e.value.code == 3
