@@ -458,6 +458,7 @@ struct cosma_gpu_oz_grouped_plan {
     std::vector<Prob> hp;
     std::vector<cosma_gpu_gemm_problem> orig;  // for the host-side recomputation of skipped problems
     std::vector<int> host_side;                // k == 0 or alpha == 0: C <- beta*C on every run
+    std::vector<int> host_ozaki;               // k beyond one exact pass: the single-problem path
     cgb::DeviceBuffer probs, maps, scheds, tiles, kitems, mitems, sitems, stats, need, ok, bad, err, exps, slices;
     int n_kitems = 0, n_mitems = 0;
     struct SplitLaunch { int S; bool kcontig; int first, count; };
@@ -555,6 +556,7 @@ int run(Plan* pl, cudaStream_t st) {
                          "grouped ozaki gemm: a pipeline wait timed out (device code " +
                              std::to_string(*pl->host_err) + ")");
     for (int i : pl->host_side) CGB_CHECK(gemm_device(desc_of(pl->orig[i]), COSMA_GPU_METHOD_NATIVE, 0, st, nullptr));
+    for (int i : pl->host_ozaki) CGB_CHECK(gemm_device(desc_of(pl->orig[i]), COSMA_GPU_METHOD_OZAKI, 0, st, nullptr));
     if (*pl->host_bad > 0) {
         // problems whose spread outgrew the planned slice count, or holding
         // Inf/NaN: their C is untouched; recompute them one by one
@@ -637,6 +639,10 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
         if (p.m == 0 || p.n == 0) continue;  // nothing to do
         if (p.k == 0 || q.alpha == 0.0) {    // C <- beta*C, on the host side of every run
             pl->host_side.push_back(i);
+            continue;
+        }
+        if (p.k > MAX_K_PER_CALL) {  // one accumulator pass is exact up to 65536 terms: the
+            pl->host_ozaki.push_back(i);  // single-problem path cuts K into exact passes
             continue;
         }
         p.S = MAX_SLICES;  // provisional: the planning pass measures what is needed

@@ -113,3 +113,26 @@ def test_grouped_ozaki_replay_with_new_data(native_lib, cuda):
             continue
         np.testing.assert_array_equal(got, oz.ozaki_gemm("N", "N", A, B, S0[i]))
     plan.close()
+
+
+def test_grouped_ozaki_long_k_goes_through_exact_passes(native_lib, cuda):
+    """A problem with k above one exact accumulator pass (65536 terms) is run
+    on the single-problem path, which cuts K into exact passes."""
+    import torch
+    from cosma_gb300 import GroupedPlan
+    shapes = [(8, 6, 70000), (50, 40, 60)]
+    probs, host = [], []
+    for i, (m, n, k) in enumerate(shapes):
+        A, B = oracle.uniform((m, k), 40 + i), oracle.uniform((k, n), 50 + i)
+        probs.append(("N", "N", m, n, k, 1.0, to_dev(A, m), m, to_dev(B, k), k, 0.0, to_dev(np.zeros((m, n)), m), m))
+        host.append((A, B))
+    plan = GroupedPlan(probs, method="ozaki", autotune=False)
+    plan.run()
+    torch.cuda.synchronize()
+    S = plan.slices()
+    assert S[0] == 0 and S[1] > 0
+    for (ta, tb, m, n, k, al, dA, lda, dB, ldb, be, dC, ldc), (A, B) in zip(probs, host):
+        got = from_dev(dC, m, n, ldc)
+        hi, lo, ab = oracle.gemm_dd("N", "N", A, B)
+        assert oracle.error_stats(got, hi, lo, ab)["max_err_over_absab"] <= 2.0 ** -51
+    plan.close()
