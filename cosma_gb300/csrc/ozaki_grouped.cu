@@ -167,32 +167,35 @@ __global__ void __launch_bounds__(256) gsplit_kernel(const Prob* __restrict__ P,
 // for which a 128 x 256 tile wastes work on padding and, above all, spends
 // its time draining accumulators into 128-bit partial sums in global memory
 // (one drain per accumulator group, ~14 per tile, each a round trip to L2).
-// At N = 64 the partial sums of a tile fit in TMEM beside two accumulators:
-//   columns [0, 64) and [64, 128): FP32 accumulators (double-buffered)
-//   columns [128 + 64w, 192 + 64w), w = 0..3: 32-bit word w of the 128-bit
-//   partial sum of each of the 64 tile columns
-// so a drain never leaves the SM.  The B slab of a stage shrinks to 8 KB, and
-// eight 24 KB stages fit in shared memory.
+// At N = 64 each of the eight epilogue threads of a row owns 32 of the tile's
+// columns, and their 128-bit partial sums fit in its registers (128 of them)
+// for the whole tile: a drain is two TMEM loads and integer adds, and the
+// accumulator goes back to the MMA issuer as soon as it has been read.  TMEM
+// holds only accumulators, G_ACC of them, so the issuer can run several
+// groups ahead of the drains.
 constexpr int GBN = 64;
-// A stage carries two consecutive 128-byte K blocks of one slice product (8
-// MMAs of 128 x 64 x 32): the wait / commit round trip of a stage costs ~300
-// cycles that the MMAs of the stage must cover, and 4 MMAs of N = 64 (48
-// cycles each) do not.  Layout of a stage: A block 0 | A block 1 | B block 0 |
-// B block 1, every part 1024-byte aligned.
-constexpr int G_STAGES = 4;
-constexpr int G_KB_PER_STAGE = 2;
+constexpr int G_ACC = 4;
+static_assert(G_ACC * GBN <= 512, "TMEM columns");
+// A stage carries three consecutive 128-byte K blocks of one slice product
+// (12 MMAs of 128 x 64 x 32): the wait / commit round trip of a stage costs
+// ~300 cycles that the MMAs of the stage must cover, and the 4 MMAs of one
+// K block (48 cycles each at N = 64) do not.  Layout of a stage: A blocks
+// 0..2 | B blocks 0..2, every part 1024-byte aligned.
+constexpr int G_STAGES = 3;
+constexpr int G_KB_PER_STAGE = 3;
+constexpr int G_KB_CHUNK = 6;  // K blocks per chunk of the group loop: two stages
 constexpr int G_A = BM * BK, G_B = GBN * BK, G_STAGE = G_KB_PER_STAGE * (G_A + G_B);
 constexpr int G_SMEM = G_STAGES * G_STAGE + 1024 + 256;
-constexpr uint32_t G_WCOL = 2 * GBN;
-static_assert(G_WCOL + 4 * GBN <= 512, "TMEM columns");
+static_assert(G_SMEM <= 232448, "grouped GEMM shared memory");
 // Eight epilogue warps, two per TMEM lane quadrant, each draining 32 of the
-// tile's 64 columns: with short K the drains, not the MMAs, set the pace.
+// tile's 64 columns.
 constexpr int G_EPI_WARPS = 8;
 constexpr int G_THREADS = 64 + 32 * G_EPI_WARPS;
+constexpr int G_COLS = GBN / 2;  // columns per epilogue thread
 
-// Drains the accumulator groups of one tile (rows mb*128.., columns
-// nb*64..) into the TMEM partial sums and, after the last group, rounds them
-// to FP64 and writes alpha*r + beta*C.
+// Drains the accumulator groups of one tile (rows mb*128.., this thread's 32
+// columns of nb*64..) into 128-bit partial sums held in registers and, after
+// the last group, rounds them to FP64 and writes alpha*r + beta*C.
 template <class Release>
 __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc, int mb, int nb, uint32_t tmem,
                                                int quad, int half, int lane, uint64_t* accf, uint32_t& acc_it,
@@ -209,58 +212,38 @@ __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc
     const int L = p.L;
     const double alpha = p.alpha, beta = p.beta;
     const bool alpha_one = p.alpha_one, beta_zero = p.beta_zero;
+    const int c0 = half * G_COLS;
+    unsigned long long lo[G_COLS], hi[G_COLS];
+#pragma unroll
+    for (int j = 0; j < G_COLS; ++j) lo[j] = hi[j] = 0ull;
     for (int g = 0; g <= last; ++g, ++acc_it) {
-        const uint32_t buf = acc_it & 1;
-        if (!__all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, err, kDevTimeoutAcc)))
+        const uint32_t buf = acc_it % G_ACC;
+        if (!__all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it / G_ACC) & 1, err, kDevTimeoutAcc)))
             return false;
         tc::tc_fence_after();
         const int sh = sc.gshift[g];
-#pragma unroll 1
-        for (int c = half * (GBN / 2); c < (half + 1) * (GBN / 2); c += 16) {
-            uint32_t v[16], w0[16], w1[16], w2[16], w3[16];
-            tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c, v);
-            if (g > 0) {
-                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 0 * GBN + c, w0);
-                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 1 * GBN + c, w1);
-                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 2 * GBN + c, w2);
-                tc::tmem_ld_32x32b_x16(tmem + lanes + G_WCOL + 3 * GBN + c, w3);
-            }
-            tc::tmem_ld_wait();
+        uint32_t v[16];
+        tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c0, v);
+        tc::tmem_ld_wait();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int x = __float2int_rn(__uint_as_float(v[j]));
-                unsigned long long lo = 0, hi = 0;
-                if (g > 0) {
-                    lo = ((unsigned long long)w1[j] << 32) | w0[j];
-                    hi = ((unsigned long long)w3[j] << 32) | w2[j];
-                }
-                add_shifted(lo, hi, x, sh);
-                if (g < last) {
-                    w0[j] = (uint32_t)lo;
-                    w1[j] = (uint32_t)(lo >> 32);
-                    w2[j] = (uint32_t)hi;
-                    w3[j] = (uint32_t)(hi >> 32);
-                } else {
-                    const int64_t gj = (int64_t)nb * GBN + c + j;
-                    if (gi < m && gj < n) {
-                        double r = i128_to_double(lo, hi, Ei + expB[gj] - L);
-                        double* cp = C + gi + gj * ldc;
-                        if (!alpha_one) r = __dmul_rn(alpha, r);
-                        if (!beta_zero) r = __dadd_rn(r, __dmul_rn(beta, *cp));
-                        tc::st_f64_hint(cp, r, pol_stream);
-                    }
-                }
-            }
-            if (g < last) {
-                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 0 * GBN + c, w0);
-                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 1 * GBN + c, w1);
-                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 2 * GBN + c, w2);
-                tc::tmem_st_32x32b_x16(tmem + lanes + G_WCOL + 3 * GBN + c, w3);
-            }
-        }
-        if (g < last) tc::tmem_st_wait();
+        for (int j = 0; j < 16; ++j) add_shifted(lo[j], hi[j], __float2int_rn(__uint_as_float(v[j])), sh);
+        tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c0 + 16, v);
+        tc::tmem_ld_wait();
         tc::tc_fence_before();
-        release(buf);
+        release(buf);  // the values are in registers: the issuer may reuse the accumulator
+#pragma unroll
+        for (int j = 0; j < 16; ++j) add_shifted(lo[16 + j], hi[16 + j], __float2int_rn(__uint_as_float(v[j])), sh);
+    }
+#pragma unroll
+    for (int j = 0; j < G_COLS; ++j) {
+        const int64_t gj = (int64_t)nb * GBN + c0 + j;
+        if (gi < m && gj < n) {
+            double r = i128_to_double(lo[j], hi[j], Ei + expB[gj] - L);
+            double* cp = C + gi + gj * ldc;
+            if (!alpha_one) r = __dmul_rn(alpha, r);
+            if (!beta_zero) r = __dadd_rn(r, __dmul_rn(beta, *cp));
+            tc::st_f64_hint(cp, r, pol_stream);
+        }
     }
     return true;
 }
@@ -280,8 +263,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     uint64_t* full = (uint64_t*)(smem + G_STAGES * G_STAGE);
     uint64_t* empty = full + G_STAGES;
     uint64_t* accf = empty + G_STAGES;
-    uint64_t* acce = accf + 2;
-    uint64_t* drain = acce + 2;
+    uint64_t* acce = accf + G_ACC;
+    uint64_t* drain = acce + G_ACC;
     uint32_t* tmem_slot = (uint32_t*)(drain + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -290,7 +273,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < G_ACC; ++b) {
             tc::mbar_init(&accf[b], 1);
             tc::mbar_init(&acce[b], 32 * G_EPI_WARPS);
         }
@@ -322,8 +305,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 tc::prefetch_tmap(tmB);
                 for (int g = 0; g < ng && ok; ++g) {
                     const int u0 = scp->gfirst[g], u1 = u0 + scp->gcount[g];
-                    for (int kc = 0; kc < kbc && ok; kc += KB_CHUNK) {
-                        const int kc1 = min(kbc, kc + KB_CHUNK);
+                    for (int kc = 0; kc < kbc && ok; kc += G_KB_CHUNK) {
+                        const int kc1 = min(kbc, kc + G_KB_CHUNK);
                         for (int u = u0; u < u1 && ok; ++u) {
                             const int arow = scp->us[u] * mpad + tl.y * BM;
                             const int brow = scp->ut[u] * npad + tl.z * GBN;
@@ -363,16 +346,16 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 const int ng = scp->n_groups;
                 for (int g = 0; g < ng && ok; ++g, ++acc_it) {
                     const int u0 = scp->gfirst[g], u1 = u0 + scp->gcount[g];
-                    const uint32_t buf = acc_it & 1;
-                    if (!tc::mbar_wait(&acce[buf], ((acc_it >> 1) & 1) ^ 1, err, kDevTimeoutAccEmpty)) {
+                    const uint32_t buf = acc_it % G_ACC;
+                    if (!tc::mbar_wait(&acce[buf], ((acc_it / G_ACC) & 1) ^ 1, err, kDevTimeoutAccEmpty)) {
                         ok = false;
                         break;
                     }
                     tc::tc_fence_after();
                     const uint32_t d_tmem = tmem + buf * GBN;
                     uint32_t accumulate = 0;
-                    for (int kc = 0; kc < kbc && ok; kc += KB_CHUNK) {
-                        const int kc1 = min(kbc, kc + KB_CHUNK);
+                    for (int kc = 0; kc < kbc && ok; kc += G_KB_CHUNK) {
+                        const int kc1 = min(kbc, kc + G_KB_CHUNK);
                         for (int u = u0; u < u1 && ok; ++u) {
                             for (int kb = kc; kb < kc1; kb += G_KB_PER_STAGE, ++it) {
                                 const int st = it % G_STAGES;
