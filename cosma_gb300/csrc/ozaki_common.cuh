@@ -92,8 +92,55 @@ __device__ __forceinline__ void finish_row(RowState s, int64_t k, int* exp_out, 
 }
 
 // --------------------------------------------------------------- slicing
+// 16 in every 5-bit field below the top digit: adding it to X turns the
+// balanced digits into plain 5-bit fields offset by 16 (see digits_of).
+template <int S>
+struct DigitOffset {
+    static constexpr unsigned long long word(int w) {
+        unsigned long long v = 0;
+        for (int p = 0; p < S - 1; ++p) {
+            const int bit = 5 * p + 4;
+            if (bit / 64 == w) v |= 1ull << (bit % 64);
+        }
+        return v;
+    }
+    static constexpr unsigned long long lo = word(0), hi = word(1);
+};
+
+// 5-bit field at bit `pos` of the 128-bit integer (hi:lo); pos is a constant.
+template <int POS>
+__device__ __forceinline__ int field5(unsigned long long lo, unsigned long long hi) {
+    if (POS + 5 <= 64) return (int)((lo >> POS) & 31ull);
+    if (POS >= 64) return (int)((hi >> (POS - 64)) & 31ull);
+    return (int)(((lo >> POS) | (hi << (64 - POS))) & 31ull);
+}
+
+template <int S, int P>
+struct DigitLoop {
+    __device__ __forceinline__ static void run(unsigned long long lo, unsigned long long hi, bool neg,
+                                               int (&d)[S]) {
+        const int dd = field5<5 * P>(lo, hi) - 16;
+        d[S - 1 - P] = neg ? -dd : dd;
+        DigitLoop<S, P + 1>::run(lo, hi, neg, d);
+    }
+};
+template <int S>
+struct DigitLoop<S, S - 1> {  // the leading digit: everything above the last field
+    __device__ __forceinline__ static void run(unsigned long long lo, unsigned long long hi, bool neg,
+                                               int (&d)[S]) {
+        constexpr int pos = 5 * (S - 1);
+        const int top = pos >= 64 ? (int)(hi >> (pos - 64)) : (int)((lo >> pos) | (hi << (64 - pos)));
+        d[0] = neg ? -top : top;
+    }
+};
+
 // Balanced base-32 digits of |x| / 2^E rounded to F = 4 + 5(S-1) fraction
 // bits (round half away from zero), most significant first, sign applied.
+// With X = round(|x| 2^(F-E)) < 2^(F+1), the digits below the top one are
+// d_p = u_p - 32 c_(p+1) with u_p = (5-bit field p of X) + c_p and carry
+// c_(p+1) = [u_p >= 16].  Adding B = sum_p 16 * 32^p to X performs exactly that
+// carry chain: field p of X + B equals u_p + 16 - 32 c_(p+1), so d_p = field_p(X + B) - 16,
+// and the leading digit is what remains above the last field.
 template <int S>
 __device__ __forceinline__ void digits_of(double x, int E, int (&d)[S]) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -110,20 +157,14 @@ __device__ __forceinline__ void digits_of(double x, int E, int (&d)[S]) {
         M = r > 63 ? 0ull : (M + (1ull << (r - 1))) >> r;
         sh = 0;
     }
-    int carry = 0;
-#pragma unroll
-    for (int p = 0; p < S; ++p) {
-        const int pos = 5 * p - sh;
-        unsigned long long v = pos >= 64 ? 0ull : (pos >= 0 ? (M >> pos) : (M << (-pos)));
-        int u = (p < S - 1) ? (int)(v & 31ull) : (int)v;
-        u += carry;
-        int dd = u;
-        if (p < S - 1) {
-            carry = u >= 16;
-            dd = carry ? u - 32 : u;
-        }
-        d[S - 1 - p] = neg ? -dd : dd;
-    }
+    // X = M << sh as a 128-bit integer (0 <= sh < F, X < 2^(F+1) <= 2^80)
+    unsigned long long xlo, xhi;
+    if (sh == 0) { xlo = M; xhi = 0; }
+    else if (sh < 64) { xlo = M << sh; xhi = M >> (64 - sh); }
+    else { xlo = 0; xhi = M << (sh - 64); }
+    const unsigned long long ylo = xlo + DigitOffset<S>::lo;
+    const unsigned long long yhi = xhi + DigitOffset<S>::hi + (ylo < xlo ? 1ull : 0ull);
+    DigitLoop<S, 0>::run(ylo, yhi, neg, d);
 }
 
 __device__ __forceinline__ uint32_t pack4_e4m3(int a, int b, int c, int e) {
