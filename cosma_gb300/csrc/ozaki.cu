@@ -690,7 +690,9 @@ struct GemmShape {
 GemmShape gemm_shape(int64_t m, int64_t n) {
     GemmShape g;
     const int64_t mt = ceil_div(m, BM), nt = ceil_div(n, BN);
-    g.pair = mt >= 2 && (mt % 2 == 0 || mt >= 10);
+    // COSMA_GPU_OZAKI_PAIR=OFF keeps every GEMM on the single-CTA form
+    static const bool pairs = env_bool("COSMA_GPU_OZAKI_PAIR", true);
+    g.pair = pairs && mt >= 2 && (mt % 2 == 0 || mt >= 10);
     if (g.pair) {
         g.cl = 2;
         g.m_pad = ceil_div(m, 2 * BM) * 2 * BM;
