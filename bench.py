@@ -283,6 +283,7 @@ def run_pdgemm(args):
            "accuracy": {"max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()), "samples": 1024},
            "e2e": {"value": flops / e2e_s / 1e12, "unit": UNIT, "h2d_bytes_per_step": (m * k + k * n + m * n) * 8,
                    "d2h_bytes_per_step": m * n * 8, "entry": "pdgemm_ (ScaLAPACK symbol), host arrays",
+                   "host_copy_route": cg.host_copy_route(A),
                    "ms_per_step": e2e_s * 1e3},
            "clocks": clocks, "gpu_launches": 4 * args.steps}
     print(json.dumps(out), flush=True)

@@ -5,7 +5,8 @@ The compute lives in the in-tree CUDA library ``_lib/libcosma_gb300.so``
 """
 from ._native import (CosmaGpuError, METHOD_AUTO, METHOD_BF16X3, METHOD_NATIVE, METHOD_OZAKI, LIB_PATH,  # noqa: F401
                       load)
-from .api import (BlockLayout, GroupedPlan, MMHandle, dgemm_ozaki_device, multiply_using_layout, descinit, gemm, gemm_device, local_multiply,  # noqa: F401
-                  make_context, pack, pxgemm, pxgemm_set_method, tiles_for_memory, unpack, zgemm_ozaki_device)
+from .api import (BlockLayout, GroupedPlan, MMHandle, dgemm_ozaki_device, multiply_using_layout, descinit, gemm,  # noqa: F401
+                  gemm_device, host_copy_route, local_multiply, make_context, pack, pxgemm, pxgemm_set_method,
+                  tiles_for_memory, unpack, zgemm_ozaki_device)
 
 __version__ = "0.1.0"

@@ -190,6 +190,23 @@ def pxgemm_set_method(method="native"):
     N.check(lib.cosma_gpu_pxgemm_set_method(N.METHODS[method] if isinstance(method, str) else int(method)))
 
 
+HOST_COPY_ROUTES = {0: "memcpy", 1: "staged", 2: "direct"}
+
+
+def host_copy_route(array):
+    """Route the host-pointer entry points take for `array` (a numpy array,
+    a torch tensor or an address): "memcpy" (device / pinned memory),
+    "staged" (pageable, through pinned buffers) or "direct" (pageable, read
+    and written in place by a device copy kernel)."""
+    if hasattr(array, "data_ptr"):
+        ptr = array.data_ptr()
+    elif hasattr(array, "ctypes"):
+        ptr = array.ctypes.data
+    else:
+        ptr = int(array)
+    return HOST_COPY_ROUTES[N.load().cosma_gpu_host_copy_route(ptr)]
+
+
 # ------------------------------------------------------ device-pointer API
 
 def gemm_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc, method="native", stream=None,

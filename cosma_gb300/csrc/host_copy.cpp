@@ -2,11 +2,16 @@
 //
 // A pageable cudaMemcpy goes through the driver's own small staging buffer
 // and one CPU thread; its speed varies widely between hosts (6.5 to 27 GB/s
-// measured on the same GB300 pool).  For pageable memory these copies stage
-// through two pinned buffers instead: host threads copy column blocks
-// into one buffer while the DMA engine moves the other, so the transfer runs
-// near the host link's pinned bandwidth.  Pinned (or registered) and device
-// memory take the direct cudaMemcpy2DAsync.
+// measured on the same GB300 pool).  These copies take one of two faster
+// routes for pageable memory:
+//  * where the GPU reaches pageable memory through the host's page tables
+//    (a Grace host's coherent NVLink-C2C link with address translation
+//    services), a device copy kernel reads or writes the host array in
+//    place, at the link's rate and without host threads;
+//  * elsewhere they stage through two pinned buffers: host threads copy
+//    column blocks into one buffer while the DMA engine moves the other.
+// COSMA_GPU_HOST_DIRECT=OFF keeps the staged route on a capable host.
+// Pinned (or registered) and device memory take cudaMemcpy2DAsync.
 #include "common.cuh"
 #include "runtime.hpp"
 
@@ -81,13 +86,50 @@ bool pageable(const void* p) {
     return at.type == cudaMemoryTypeUnregistered;
 }
 
+// Whether kernels may dereference pageable host pointers (the device
+// accesses pageable memory, and does so through the host's page tables).
+bool host_direct() {
+    static const bool capable = [] {
+        int dev = 0, pma = 0, hpt = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return pma == 1 && hpt == 1;
+    }();
+    return capable && env_bool("COSMA_GPU_HOST_DIRECT", true);
+}
+
+// The widest element (8 or 4 bytes) dividing both addresses, both pitches
+// and the width of a copy; 0 when none does.
+int copy_elem(const void* a, const void* b, size_t pa, size_t pb, size_t width) {
+    const uintptr_t x = (uintptr_t)a | (uintptr_t)b | (uintptr_t)pa | (uintptr_t)pb | (uintptr_t)width;
+    return x % 8 == 0 ? 8 : x % 4 == 0 ? 4 : 0;
+}
+
+// The copy as a device kernel (op N pack, 16-byte vectors where aligned);
+// false when the layout does not fit one.
+bool direct_copy(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols, cudaStream_t s,
+                 int* status) {
+    const int eb = copy_elem(dst, src, dpitch, spitch, width);
+    if (!eb) return false;
+    *status = pack_device(0, false, eb, (int64_t)(width / eb), (int64_t)cols, src, (int64_t)(spitch / eb), dst,
+                          (int64_t)(dpitch / eb), s);
+    return true;
+}
+
 }  // namespace
 
 int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s) {
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    const bool pg = pageable(src);
+    int st = COSMA_GPU_SUCCESS;
+    if (pg && host_direct() && direct_copy(dst, dpitch, src, spitch, width, cols, s, &st)) return st;
     std::lock_guard<std::mutex> lock(g_stage_mu);
-    if (!pageable(src) || width > kStageBytes || !stager_ready()) {
+    if (!pg || width > kStageBytes || !stager_ready()) {
         CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, s));
         return COSMA_GPU_SUCCESS;
     }
@@ -107,8 +149,15 @@ int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
 int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s) {
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    const bool pg = pageable(dst);
+    int st = COSMA_GPU_SUCCESS;
+    if (pg && host_direct() && direct_copy(dst, dpitch, src, spitch, width, cols, s, &st)) {
+        CGB_CHECK(st);
+        CGB_CUDA(cudaStreamSynchronize(s));
+        return COSMA_GPU_SUCCESS;
+    }
     std::lock_guard<std::mutex> lock(g_stage_mu);
-    if (!pageable(dst) || width > kStageBytes || !stager_ready()) {
+    if (!pg || width > kStageBytes || !stager_ready()) {
         CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, cudaMemcpyDeviceToHost, s));
         CGB_CUDA(cudaStreamSynchronize(s));
         return COSMA_GPU_SUCCESS;
@@ -134,3 +183,8 @@ int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
 }
 
 }  // namespace cgb
+
+extern "C" int cosma_gpu_host_copy_route(const void* ptr) {
+    if (!cgb::pageable(ptr)) return 0;
+    return cgb::host_direct() ? 2 : 1;
+}

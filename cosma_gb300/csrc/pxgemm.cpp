@@ -27,11 +27,6 @@
 extern "C" void Cblacs_gridinfo(int ctxt, int* nprow, int* npcol, int* myrow, int* mycol) __attribute__((weak));
 
 namespace cgb {
-int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t cols, const void* src, int64_t lds,
-                void* dst, int64_t ldd, cudaStream_t s);
-int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
-                  const double* beta, void* dst, int64_t ldd, cudaStream_t s);
-
 namespace {
 
 std::mutex g_px_mu;

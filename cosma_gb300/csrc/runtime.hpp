@@ -74,16 +74,21 @@ int ozaki_zgemm(const GemmDesc& g, int slices, cudaStream_t stream,
                 cosma_gpu_ozaki_info* info);                     // ozaki.cu
 int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
                   const double* beta, void* dst, int64_t ldd, cudaStream_t s);  // layout.cu
+// dst = op(src) (op 0 N, 1 T, 2 C, 3 conjugate), column-major; any pointer the
+// device can dereference (layout.cu)
+int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t cols, const void* src, int64_t lds,
+                void* dst, int64_t ldd, cudaStream_t s);
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
 
 // The method of the process-wide entry points (p?gemm, multiply_using_layout):
 // cosma_gpu_pxgemm_set_method, else COSMA_GPU_GEMM_METHOD (pxgemm.cpp).
 int process_gemm_method();
 
-// Column-major sub-matrix copies between host and HBM (host_copy.cpp):
-// pageable host memory goes through pinned staging buffers filled by
-// several host threads; pinned / device memory is copied directly.  The D2H
-// form returns once the data is in host memory.
+// Column-major sub-matrix copies between host and HBM (host_copy.cpp).
+// Pageable host memory is copied by a device kernel where the GPU reads the
+// host's page tables, else through pinned staging buffers filled by several
+// host threads; pinned / device memory is copied directly.  The D2H form
+// returns once the data is in host memory.
 int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s);
 int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,

@@ -381,6 +381,16 @@ void COSMA_PZGEMM_(COSMA_GPU_PXGEMM_ARGS(double));
  * sets the initial value). */
 int cosma_gpu_pxgemm_set_method(int method);
 
+/* Route a host <-> HBM copy of the array at `ptr` takes inside the
+ * host-pointer entry points (p?gemm, multiply_using_layout):
+ *   0  cudaMemcpy (device, pinned or registered memory);
+ *   1  pageable memory through pinned staging buffers filled by host threads;
+ *   2  pageable memory read / written in place by a device copy kernel (the
+ *      GPU reaches pageable memory through the host's page tables, as on a
+ *      Grace host; COSMA_GPU_HOST_DIRECT=OFF selects route 1 instead).
+ * New: COSMA stages through its own pinned buffers (src/cosma/pinned_buffers.cpp). */
+int cosma_gpu_host_copy_route(const void* ptr);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,12 +122,17 @@ def test_psgemm(native_lib, cuda):
               dtype=np.float32)
 
 
-def test_large_host_arrays_through_staged_copies(native_lib, cuda):
+@pytest.mark.parametrize("direct", ["ON", "OFF"])
+def test_large_host_arrays_through_staged_copies(native_lib, cuda, monkeypatch, direct):
     """Host (pageable) operands larger than one pinned staging buffer
-    (128 MiB) travel in several chunks; the result must be bit-identical to
-    the same pdgemm on device arrays, and C outside the sub-matrix untouched."""
+    (128 MiB): with COSMA_GPU_HOST_DIRECT=OFF they travel in several staged
+    chunks; with it ON (where the GPU reads the host's page tables) a device
+    kernel copies them in place.  Either way the result must be
+    bit-identical to the same pdgemm on device arrays, and C outside the
+    sub-matrix untouched."""
     import torch
-    from cosma_gb300 import descinit, pxgemm
+    from cosma_gb300 import descinit, host_copy_route, load, pxgemm
+    monkeypatch.setenv("COSMA_GPU_HOST_DIRECT", direct)
     m, n, k = 1500, 1300, 12000            # A^T: 12000 x 1500 x 8 B = 144 MB, B: 125 MB
     lda, ldb, ldc = k + 3, k, m + 5
     A = oracle.uniform((lda, m), 11)
@@ -145,3 +150,28 @@ def test_large_host_arrays_through_staged_copies(native_lib, cuda):
     dev = dC.cpu().numpy().reshape(n + 2, ldc).T
     assert Ch.tobytes() == np.asfortranarray(dev).tobytes()
     assert Ch[:, 0].tobytes() == C[:, 0].tobytes()   # column outside jc..jc+n-1
+    route = host_copy_route(A)
+    assert route == ("staged" if direct == "OFF" else route)
+    assert route in ("staged", "direct")
+    assert host_copy_route(dA) == "memcpy"
+
+
+def test_host_direct_copies_odd_layouts(native_lib, cuda, monkeypatch):
+    """The in-place device copy handles 4-byte alignment (psgemm with odd
+    leading dimensions and offsets) and bit-matches the staged route."""
+    from cosma_gb300 import descinit, pxgemm
+    m, n, k = 37, 29, 53
+    lda, ldb, ldc = k + 1, k + 3, m + 7
+    A = oracle.uniform((lda, m + 1), 21, dtype=np.float32)
+    B = oracle.uniform((ldb, n + 2), 22, dtype=np.float32)
+    C = oracle.uniform((ldc, n + 1), 23, dtype=np.float32)
+    desca = descinit(lda, m + 1, 8, 8, 0, 0, 0, lda)
+    descb = descinit(ldb, n + 2, 8, 8, 0, 0, 0, ldb)
+    descc = descinit(ldc, n + 1, 8, 8, 0, 0, 0, ldc)
+    outs = []
+    for direct in ("OFF", "ON"):
+        monkeypatch.setenv("COSMA_GPU_HOST_DIRECT", direct)
+        Ch = C.copy(order="F")
+        pxgemm("T", "N", m, n, k, 1.0, A, 2, 2, desca, B, 1, 3, descb, 0.5, Ch, 3, 2, descc)
+        outs.append(Ch.tobytes())
+    assert outs[0] == outs[1]
