@@ -821,6 +821,22 @@ def main():
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_val = flops * world / e2e_s / 1e12
+    # the same call on the caller's pageable arrays (no pinned copies made)
+    del hA, hB, hC
+    pA, pB = np.asfortranarray(A), np.asfortranarray(B)
+    pC = np.empty((n, n), order="F")
+    t0 = time.perf_counter()
+    cg.gemm(h, "N", "N", n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)  # first use of these allocations
+    first_s = time.perf_counter() - t0
+    cg.gemm(h, "N", "N", n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        cg.gemm(h, "N", "N", n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
+    barrier()
+    pageable_s = (time.perf_counter() - t0) / 3
+    pageable_route = cg.host_copy_route(pA)
+    del pA, pB, pC
     h.close()
 
     # exponent-spread variants (one step each)
@@ -883,7 +899,11 @@ def main():
            "variants": variants, "roofline": roofline, "clocks": clocks,
            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
                    "entry": "cosma_gpu_tmm_gemm_d (Tiled-MM gpu::gemm drop-in), pinned host A/B/C",
-                   "ms_per_step": e2e_s * 1e3},
+                   "ms_per_step": e2e_s * 1e3,
+                   "pageable": {"value": flops * world / pageable_s / 1e12, "ms_per_step": pageable_s * 1e3,
+                                "first_call_ms": first_s * 1e3, "host_copy_route": pageable_route,
+                                "note": "same call on the caller's pageable numpy arrays: 2 warm-up calls "
+                                        "(the first one on fresh allocations timed apart), mean of 3"}},
            "gpu_launches": KERNELS_PER_STEP * args.steps}
     if rank == 0:
         tflops_cpu, kb, cdt = cpu_dgemm_sample(A, B)

@@ -93,6 +93,15 @@ int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
                 cudaStream_t s);
 int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s);
+// Asynchronous 2-D copy on stream s: a pageable host side goes through the
+// device copy kernel where the GPU reads the host's page tables, everything
+// else through cudaMemcpy2DAsync (pageable memory then takes the driver's
+// own staging).  Nothing is waited for.
+int copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                  cudaMemcpyKind kind, cudaStream_t s);
+// Whether the device copy kernel route is on (capable device, and
+// COSMA_GPU_HOST_DIRECT not OFF).
+bool host_direct_available();
 
 // Grouped Ozaki-split FP64 GEMM (ozaki_grouped.cu), driven by the grouped
 // plan of grouped.cu when it is created with the Ozaki method.

@@ -21,6 +21,9 @@
 // the matrices cross the C2C link exactly once; larger problems stream tiles
 // over several streams so that copies of one tile overlap the GEMM of
 // another.  Device pointers are detected and used in place (no copies).
+// On a Grace host the GPU reaches pageable memory through the host's page
+// tables: tiles of pageable matrices are then copied in place by a device
+// kernel and the pin flag registers nothing.
 #include "common.cuh"
 #include "runtime.hpp"
 
@@ -115,8 +118,7 @@ size_t span_bytes(int64_t rows, int64_t cols, int64_t ld, size_t es) {
 int copy2d(void* dst, int64_t dld, const void* src, int64_t sld, int64_t rows, int64_t cols, size_t es,
            cudaMemcpyKind kind, cudaStream_t s) {
     if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
-    CGB_CUDA(cudaMemcpy2DAsync(dst, (size_t)dld * es, src, (size_t)sld * es, (size_t)rows * es, (size_t)cols, kind, s));
-    return COSMA_GPU_SUCCESS;
+    return copy_2d_async(dst, (size_t)dld * es, src, (size_t)sld * es, (size_t)rows * es, (size_t)cols, kind, s);
 }
 
 bool is_zero(const double* v, Scalar s) { return v[0] == 0.0 && (!scalar_complex(s) || v[1] == 0.0); }
@@ -176,7 +178,11 @@ int tmm_gemm(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int64_t m, int
     }
 
     std::vector<void*> scoped;
-    if (pin) {
+    // Where kernels copy pageable memory in place, registering it only adds
+    // cost: cudaHostRegister of 6 GB took 70 to 800 ms per call, while the
+    // in-place copies run at the link's rate (16384^3 Ozaki DGEMM from
+    // pageable arrays: 315 ms unregistered against 354 to 1083 ms registered).
+    if (pin && !host_direct_available()) {
         if (!dA && !trivial) pin_range(h, A, span_bytes(a_rows, a_cols, lda, es), scoped);
         if (!dB && !trivial) pin_range(h, B, span_bytes(b_rows, b_cols, ldb, es), scoped);
         if (!dC) pin_range(h, C, span_bytes(m, n, ldc, es), scoped);

@@ -164,3 +164,40 @@ def test_invalid_arguments_raise(native_lib, cuda):
         gemm_device("X", "N", 2, 2, 2, 1.0, d, 2, d, 2, 0.0, d, 2, scalar="d")
     with pytest.raises(CosmaGpuError):
         gemm_device("N", "N", 4, 2, 2, 1.0, d, 2, d, 2, 0.0, d, 2, scalar="d")  # lda < m
+
+
+@pytest.mark.parametrize("scalar", ["d", "s", "z"])
+def test_tiled_mm_pageable_tiles_in_place_and_staged(native_lib, cuda, monkeypatch, scalar):
+    """Tiles of pageable matrices with odd leading dimensions stream through
+    either host route (device copy kernel in place, or the driver's pageable
+    copies with the pin flag registering them): both give bit-identical C,
+    matching the same tiling on device pointers."""
+    import torch
+    from cosma_gb300 import gemm, make_context
+    dt = {"d": np.float64, "s": np.float32, "z": np.complex128}[scalar]
+    m, n, k = 301, 203, 257
+    lda, ldb, ldc = m + 3, k + 1, m + 5
+    rng = np.random.default_rng(5)
+
+    def mat(r, c):
+        x = rng.uniform(-1, 1, (r, c))
+        if scalar == "z":
+            x = x + 1j * rng.uniform(-1, 1, (r, c))
+        return np.asfortranarray(x.astype(dt))
+    A, B, C0 = mat(lda, k), mat(ldb, n), mat(ldc, n)
+    alpha, beta = (0.75, -0.5) if scalar != "z" else (0.75 - 0.25j, 0.5 + 1j)
+    outs = []
+    for direct, pin in (("ON", True), ("OFF", True), ("OFF", False)):
+        monkeypatch.setenv("COSMA_GPU_HOST_DIRECT", direct)
+        h = make_context(scalar, 3, 96, 64, 80)
+        Cg = C0.copy(order="F")
+        gemm(h, "N", "N", m, n, k, alpha, A, lda, B, ldb, beta, Cg, ldc, pin_host_buffers=pin)
+        h.close()
+        outs.append(Cg.tobytes())
+    assert outs[0] == outs[1] == outs[2]
+    h = make_context(scalar, 3, 96, 64, 80)
+    dB = torch.from_numpy(B.reshape(-1, order="F").copy()).cuda()
+    Ch = C0.copy(order="F")
+    gemm(h, "N", "N", m, n, k, alpha, A, lda, dB, ldb, beta, Ch, ldc)   # mixed host / device operands
+    h.close()
+    assert Ch.tobytes() == outs[0]
