@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cctype>
+#include <dlfcn.h>
 #include <mutex>
 #include <string>
 
@@ -176,26 +177,60 @@ int process_gemm_method() {
 
 }  // namespace cgb
 
+namespace cgb {
+namespace {
+
+// COSMA_DIM_THRESHOLD (default 0, i.e. never): a problem with
+// min(m, n, k) below it goes to the next p?gemm_ in the dynamic symbol
+// search order, the real ScaLAPACK linked after this library, as the
+// reference's interposed entry points do (src/cosma/pxgemm.cpp,
+// src/cosma/cosma_pxgemm.cpp:652-655, default in
+// src/cosma/environment_variables.hpp:92).  Without a next definition the
+// problem stays here.
+bool too_small(const int* m, const int* n, const int* k) {
+    const long long t = env_ll("COSMA_DIM_THRESHOLD", 0);
+    if (t <= 0 || !m || !n || !k) return false;
+    return (long long)std::min(*m, std::min(*n, *k)) < t;
+}
+
+void* next_definition(const char* name) { return dlsym(RTLD_NEXT, name); }
+
+}  // namespace
+}  // namespace cgb
+
 // The ScaLAPACK entry points are void (as in the reference); their status is
-// available through cosma_gpu_last_error().
-#define CGB_PX_REAL(NAME, T, SC)                                                                                     \
+// available through cosma_gpu_last_error().  Every spelling falls through to
+// the Fortran symbol REAL (p?gemm_) of the next library.
+#define CGB_PX_NEXT(T, REAL)                                                                                         \
+    if (cgb::too_small(m, n, k)) {                                                                                   \
+        using Next = void (*)(COSMA_GPU_PXGEMM_ARGS(T));                                                            \
+        static const Next next = (Next)cgb::next_definition(#REAL);                                                  \
+        if (next) {                                                                                                  \
+            cgb::clear_error();                                                                                      \
+            next(transa, transb, m, n, k, alpha, a, ia, ja, desca, b, ib, jb, descb, beta, c, ic, jc, descc);        \
+            return;                                                                                                  \
+        }                                                                                                            \
+    }
+#define CGB_PX_REAL(NAME, T, SC, REAL)                                                                               \
     void NAME(COSMA_GPU_PXGEMM_ARGS(T)) {                                                                           \
+        CGB_PX_NEXT(T, REAL)                                                                                         \
         cgb::clear_error();                                                                                          \
         double al[2] = {alpha ? (double)alpha[0] : 0.0, 0.0}, be[2] = {beta ? (double)beta[0] : 0.0, 0.0};          \
         cgb::pxgemm_impl(SC, transa, transb, m, n, k, al, a, ia, ja, desca, b, ib, jb, descb, be, c, ic, jc, descc); \
     }
-#define CGB_PX_CPLX(NAME, T, SC)                                                                                     \
+#define CGB_PX_CPLX(NAME, T, SC, REAL)                                                                               \
     void NAME(COSMA_GPU_PXGEMM_ARGS(T)) {                                                                           \
+        CGB_PX_NEXT(T, REAL)                                                                                         \
         cgb::clear_error();                                                                                          \
         double al[2] = {alpha ? (double)alpha[0] : 0.0, alpha ? (double)alpha[1] : 0.0};                            \
         double be[2] = {beta ? (double)beta[0] : 0.0, beta ? (double)beta[1] : 0.0};                                \
         cgb::pxgemm_impl(SC, transa, transb, m, n, k, al, a, ia, ja, desca, b, ib, jb, descb, be, c, ic, jc, descc); \
     }
-#define CGB_PX_FAMILY(NS, ND, NC, NZ)                 \
-    CGB_PX_REAL(NS, float, cgb::Scalar::S)           \
-    CGB_PX_REAL(ND, double, cgb::Scalar::D)          \
-    CGB_PX_CPLX(NC, float, cgb::Scalar::C)           \
-    CGB_PX_CPLX(NZ, double, cgb::Scalar::Z)
+#define CGB_PX_FAMILY(NS, ND, NC, NZ)                          \
+    CGB_PX_REAL(NS, float, cgb::Scalar::S, psgemm_)           \
+    CGB_PX_REAL(ND, double, cgb::Scalar::D, pdgemm_)          \
+    CGB_PX_CPLX(NC, float, cgb::Scalar::C, pcgemm_)           \
+    CGB_PX_CPLX(NZ, double, cgb::Scalar::Z, pzgemm_)
 
 extern "C" {
 
