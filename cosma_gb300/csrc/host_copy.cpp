@@ -78,14 +78,22 @@ void parallel_copy(char* dst, size_t dpitch, const char* src, size_t spitch, siz
     for (auto& x : th) x.join();
 }
 
-bool pageable(const void* p) {
+enum class HostMem { Device, PinnedMapped, PinnedOther, Pageable };
+
+// What kind of memory p is.  PinnedMapped: page-locked host memory that
+// kernels reach under its own address (unified addressing).
+HostMem host_mem(const void* p) {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
-        return true;
+        return HostMem::Pageable;
     }
-    return at.type == cudaMemoryTypeUnregistered;
+    if (at.type == cudaMemoryTypeUnregistered) return HostMem::Pageable;
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer == p ? HostMem::PinnedMapped : HostMem::PinnedOther;
+    return HostMem::Device;
 }
+
+bool pageable(const void* p) { return host_mem(p) == HostMem::Pageable; }
 
 // Whether kernels may dereference pageable host pointers (the device
 // accesses pageable memory, and does so through the host's page tables).
@@ -147,15 +155,26 @@ void prefault(const void* base, size_t pitch, size_t width, size_t cols, bool wr
     for (auto& x : th) x.join();
 }
 
-// The copy as a device kernel (op N pack, 16-byte vectors where aligned),
-// after faulting in the host side's pages; false when the layout does not
-// fit one.
+// The copy as a device kernel (op N pack, 16-byte vectors where aligned)
+// when the host side is pageable or mapped pinned memory and the device
+// reaches host memory through the host's page tables.  On such a host (a
+// Grace CPU on NVLink-C2C) the kernel also beats the copy engines on pinned
+// memory: a 16384^3 Ozaki DGEMM from torch-pinned buffers took 305 to 313 ms
+// with kernel copies against 329 to 342 ms with cudaMemcpy.  Pageable pages
+// are faulted in first.  False, having done nothing, when the route does not
+// apply.
 bool direct_copy(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols, bool host_is_dst,
                  cudaStream_t s, int* status) {
+    const void* host = host_is_dst ? (const void*)dst : src;
+    const HostMem hm = host_mem(host);
+    if (hm != HostMem::Pageable && hm != HostMem::PinnedMapped) return false;
+    if (!host_direct()) return false;
     const int eb = copy_elem(dst, src, dpitch, spitch, width);
     if (!eb) return false;
-    if (host_is_dst) prefault(dst, dpitch, width, cols, true);
-    else prefault(src, spitch, width, cols, false);
+    if (hm == HostMem::Pageable) {
+        if (host_is_dst) prefault(dst, dpitch, width, cols, true);
+        else prefault(src, spitch, width, cols, false);
+    }
     *status = pack_device(0, false, eb, (int64_t)(width / eb), (int64_t)cols, src, (int64_t)(spitch / eb), dst,
                           (int64_t)(dpitch / eb), s);
     return true;
@@ -166,9 +185,9 @@ bool direct_copy(void* dst, size_t dpitch, const void* src, size_t spitch, size_
 int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s) {
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
-    const bool pg = pageable(src);
     int st = COSMA_GPU_SUCCESS;
-    if (pg && host_direct() && direct_copy(dst, dpitch, src, spitch, width, cols, false, s, &st)) return st;
+    if (direct_copy(dst, dpitch, src, spitch, width, cols, false, s, &st)) return st;
+    const bool pg = pageable(src);
     std::lock_guard<std::mutex> lock(g_stage_mu);
     if (!pg || width > kStageBytes || !stager_ready()) {
         CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, s));
@@ -190,13 +209,13 @@ int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
 int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s) {
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
-    const bool pg = pageable(dst);
     int st = COSMA_GPU_SUCCESS;
-    if (pg && host_direct() && direct_copy(dst, dpitch, src, spitch, width, cols, true, s, &st)) {
+    if (direct_copy(dst, dpitch, src, spitch, width, cols, true, s, &st)) {
         CGB_CHECK(st);
         CGB_CUDA(cudaStreamSynchronize(s));
         return COSMA_GPU_SUCCESS;
     }
+    const bool pg = pageable(dst);
     std::lock_guard<std::mutex> lock(g_stage_mu);
     if (!pg || width > kStageBytes || !stager_ready()) {
         CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, cudaMemcpyDeviceToHost, s));
@@ -232,9 +251,7 @@ int copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
     const void* host = kind == cudaMemcpyHostToDevice ? src : kind == cudaMemcpyDeviceToHost ? dst : nullptr;
     int st = COSMA_GPU_SUCCESS;
-    if (host && pageable(host) && host_direct() &&
-        direct_copy(dst, dpitch, src, spitch, width, cols, host == dst, s, &st))
-        return st;
+    if (host && direct_copy(dst, dpitch, src, spitch, width, cols, host == dst, s, &st)) return st;
     CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, s));
     return COSMA_GPU_SUCCESS;
 }
@@ -244,6 +261,9 @@ bool host_direct_available() { return host_direct(); }
 }  // namespace cgb
 
 extern "C" int cosma_gpu_host_copy_route(const void* ptr) {
-    if (!cgb::pageable(ptr)) return 0;
-    return cgb::host_direct() ? 2 : 1;
+    const cgb::HostMem hm = cgb::host_mem(ptr);
+    const bool direct = cgb::host_direct();
+    if (hm == cgb::HostMem::Pageable) return direct ? 2 : 1;
+    if (hm == cgb::HostMem::PinnedMapped && direct) return 2;
+    return 0;
 }

@@ -110,9 +110,9 @@ struct DigitOffset {
 // 5-bit field at bit `pos` of the 128-bit integer (hi:lo); pos is a constant.
 template <int POS>
 __device__ __forceinline__ int field5(unsigned long long lo, unsigned long long hi) {
-    if (POS + 5 <= 64) return (int)((lo >> POS) & 31ull);
-    if (POS >= 64) return (int)((hi >> (POS - 64)) & 31ull);
-    return (int)(((lo >> POS) | (hi << (64 - POS))) & 31ull);
+    if constexpr (POS + 5 <= 64) return (int)((lo >> POS) & 31ull);
+    else if constexpr (POS >= 64) return (int)((hi >> (POS - 64)) & 31ull);
+    else return (int)(((lo >> POS) | (hi << (64 - POS))) & 31ull);
 }
 
 template <int S, int P>

@@ -385,9 +385,10 @@ int cosma_gpu_pxgemm_set_method(int method);
  * host-pointer entry points (p?gemm, multiply_using_layout):
  *   0  cudaMemcpy (device, pinned or registered memory);
  *   1  pageable memory through pinned staging buffers filled by host threads;
- *   2  pageable memory read / written in place by a device copy kernel (the
- *      GPU reaches pageable memory through the host's page tables, as on a
- *      Grace host; COSMA_GPU_HOST_DIRECT=OFF selects route 1 instead).
+ *   2  a device copy kernel reading / writing the host array in place, for
+ *      pageable and for mapped pinned memory, where the GPU reaches host
+ *      memory through the host's page tables, as on a Grace host
+ *      (COSMA_GPU_HOST_DIRECT=OFF selects routes 1 and 0 instead).
  * New: COSMA stages through its own pinned buffers (src/cosma/pinned_buffers.cpp). */
 int cosma_gpu_host_copy_route(const void* ptr);
 

@@ -165,6 +165,39 @@ def test_tiled_mm_handle_with_ozaki_method(native_lib, cuda):
     h.close()
 
 
+@pytest.mark.parametrize("direct", ["ON", "OFF"])
+def test_handle_host_c_matches_device_path(native_lib, cuda, monkeypatch, direct):
+    """A whole-problem Ozaki DGEMM through the handle on host operands
+    (pageable numpy and torch-pinned C, beta 0 and beta != 0, op T on A),
+    over either host copy route: bit-identical to the same GEMM on device
+    pointers, with C's bytes crossing the link once each way."""
+    import torch
+    from cosma_gb300 import dgemm_ozaki_device, gemm, host_copy_route, make_context
+    monkeypatch.setenv("COSMA_GPU_HOST_DIRECT", direct)
+    m, n, k = 700, 515, 900
+    A, B = oracle.uniform((k, m), 41), oracle.uniform((k, n), 42)   # op(A) = A^T
+    C0 = oracle.uniform((m + 3, n), 43)
+    dA = torch.from_numpy(A.reshape(-1, order="F").copy()).cuda()
+    dB = torch.from_numpy(B.reshape(-1, order="F").copy()).cuda()
+    for beta in (0.0, -0.75):
+        dC = torch.from_numpy(C0.reshape(-1, order="F").copy()).cuda()
+        dgemm_ozaki_device("T", "N", m, n, k, 1.5, dA, k, dB, k, beta, dC, m + 3)
+        ref = dC.cpu().numpy().reshape(n, m + 3).T
+        h = make_context("d", 2, 0, 0, 0)
+        h.set_method("ozaki", 0)
+        Cp = C0.copy(order="F")
+        gemm(h, "T", "N", m, n, k, 1.5, A, k, B, k, beta, Cp, m + 3)
+        assert Cp.tobytes() == np.asfortranarray(ref).tobytes()
+        h2d, d2h = h.transfer_bytes()
+        assert d2h == m * n * 8
+        assert h2d == A.nbytes + B.nbytes + (m * n * 8 if beta != 0 else 0)
+        pinned = torch.from_numpy(C0.reshape(-1, order="F").copy()).pin_memory()
+        assert host_copy_route(pinned) == ("memcpy" if direct == "OFF" else host_copy_route(pinned))
+        gemm(h, "T", "N", m, n, k, 1.5, A, k, B, k, beta, pinned, m + 3)
+        assert pinned.numpy().tobytes() == np.asfortranarray(ref).reshape(-1, order="F").tobytes()
+        h.close()
+
+
 def test_memory_limited_handle_streams_in_tiles(native_lib, cuda):
     """A handle under a 256 MiB device budget runs a larger Ozaki DGEMM from
     host memory in tiles: the operands travel several times and the result
