@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--phi", type=int, default=0)
     p.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison run")
     p.add_argument("--no-variants", action="store_true", help="skip the phi = 8 / 32 variants")
+    p.add_argument("--count", type=int, default=10000,
+                   help="problems in the grouped configuration (10,000; fewer for profiler captures)")
     p.add_argument("--config", default="precision",
                    choices=["precision", "plain", "pdgemm", "sgemm", "grouped", "stream"],
                    help="precision: the headline line; pdgemm: the 1x1 ScaLAPACK configuration; "
@@ -370,7 +372,7 @@ def run_grouped(args):
     import cosma_gb300 as cg
 
     dev = torch.device("cuda", 0)
-    count = 10000
+    count = args.count
     rng = np.random.default_rng(2024)
     draw = lambda: np.clip(np.round(np.exp(rng.uniform(np.log(16), np.log(1024), count))), 16, 1024).astype(np.int64)
     m, n, k = draw(), draw(), draw()
@@ -477,7 +479,7 @@ def run_grouped(args):
            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic U[-1,1], seeded",
-           "config": {"workload": "batching: 10,000 FP64 GEMMs, m,n,k log-uniform in [16,1024], random N/T",
+           "config": {"workload": f"batching: {count:,} FP64 GEMMs, m,n,k log-uniform in [16,1024], random N/T",
                       "useful_gflop": useful / 1e9},
            "plan": info, "plan_build_s": plan_s,
            "frac_of_native_fp64": value / native_peak, "native_fp64_tflops_4096": native_peak,
