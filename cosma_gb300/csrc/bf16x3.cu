@@ -279,15 +279,7 @@ Workspace* workspace(cudaStream_t s) {
     return w;
 }
 
-int num_sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = kNumSMs;
-    }
-    return n;
-}
+int num_sms() { return device_sm_count(); }
 
 }  // namespace b3
 
@@ -338,11 +330,16 @@ int bf16x3_sgemm(const GemmDesc& g, cudaStream_t st) {
                            (uint64_t)k_pad * 2, BKE, BM));
     CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, sb, (uint64_t)k_pad, (uint64_t)(3 * n_pad),
                            (uint64_t)k_pad * 2, BKE, BN));
-    static bool attr = false;
-    if (!attr) {
-        CGB_CUDA(cudaFuncSetAttribute(bf16x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        attr = true;
-    }
+    static PerDevice<bool> attr;  // the attribute is set once per device
+    bool done = false;
+    CGB_CHECK(attr.get(
+        [](bool& v) {
+            CGB_CUDA(cudaFuncSetAttribute(bf16x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          SMEM_BYTES));
+            v = true;
+            return COSMA_GPU_SUCCESS;
+        },
+        &done));
     const int grid = std::min(p.num_tiles, num_sms());
     bf16x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
     CGB_CUDA(cudaGetLastError());

@@ -224,11 +224,15 @@ int launch_typed(const Args& a, cudaStream_t stream) {
     using T = Tile<E, TA, TB>;
     constexpr int smem = STAGES * T::STAGE_BYTES;
     auto kern = dmma_gemm_kernel<E, TA, TB>;
-    static bool configured = false;  // attribute set once per process (single device use)
-    if (!configured) {
-        CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        configured = true;
-    }
+    static PerDevice<bool> configured;  // the attribute is set once per device
+    bool done = false;
+    CGB_CHECK(configured.get(
+        [&](bool& v) {
+            CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            v = true;
+            return COSMA_GPU_SUCCESS;
+        },
+        &done));
     dim3 grid((unsigned)ceil_div(a.m, BM), (unsigned)ceil_div(a.n, BN));
     if (grid.y > 65535) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "native gemm: n too large");
     kern<<<grid, THREADS, smem, stream>>>(a);

@@ -98,16 +98,24 @@ bool pageable(const void* p) { return host_mem(p) == HostMem::Pageable; }
 // Whether kernels may dereference pageable host pointers (the device
 // accesses pageable memory, and does so through the host's page tables).
 bool host_direct() {
-    static const bool capable = [] {
-        int dev = 0, pma = 0, hpt = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        return pma == 1 && hpt == 1;
-    }();
+    static PerDevice<bool> cache;  // a property of the current device
+    bool capable = false;
+    if (cache.get(
+            [](bool& v) {
+                int dev = 0, pma = 0, hpt = 0;
+                v = false;
+                if (cudaGetDevice(&dev) != cudaSuccess ||
+                    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+                    cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) !=
+                        cudaSuccess) {
+                    cudaGetLastError();
+                    return 0;
+                }
+                v = pma == 1 && hpt == 1;
+                return 0;
+            },
+            &capable) != 0)
+        capable = false;
     return capable && env_bool("COSMA_GPU_HOST_DIRECT", true);
 }
 

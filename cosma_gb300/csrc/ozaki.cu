@@ -37,8 +37,8 @@
 // TMEM so that the epilogue of one accumulator group overlaps the MMAs of the
 // next.  Two forms: CTA pairs on 256 x 256 tiles (tcgen05 cta_group::2, 32 KB
 // per stage and CTA) whenever m spans two or more 128-row tiles, else single
-// CTAs on 128 x 256 tiles (48 KB per stage) in clusters along N that share
-// the A slab by TMA multicast.
+// CTAs on 128 x 256 tiles (48 KB per stage).  Every CTA loads its own operand
+// tiles; no TMA load is multicast.
 //   warp 0      TMA producer         warp 1   TMEM owner + MMA issuer
 //   warps 2..5  epilogue (TMEM -> registers -> 128-bit integer sums)
 #include "common.cuh"
@@ -210,20 +210,9 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
 }
 
 // ------------------------------------------------------------------ GEMM
-// Clusters of CL CTAs along N: the CL CTAs of a cluster compute the tiles
-// (mb, CL*c + 0 .. CL*c + CL-1) of one cluster tile (mb, c) in lockstep.  They
-// share the A slab of every K block: each CTA loads rows [r*128/CL, (r+1)*128/CL)
-// of it and multicasts them to the whole cluster, so an A panel leaves HBM (or
-// L2) once per cluster instead of once per CTA; B stays per CTA.  Every MMA
-// commit that frees a stage is multicast to the `empty` barriers of all CTAs of
-// the cluster (a CTA may only refill a stage once every peer is done with it).
-template <int CL>
-__device__ __forceinline__ void cluster_tile_coords(int ctile, int num_m, int num_n, int rank, int& mb, int& nb) {
-    tile_coords(ctile, num_m, num_n / CL, mb, nb);
-    nb = nb * CL + rank;
-}
-
-template <int CL>
+// Single-CTA form on 128 x 256 tiles, used when m spans fewer than two
+// 128-row tiles (or an odd number below ten): each CTA loads its own A and B
+// tiles of every K block.
 __global__ void __launch_bounds__(THREADS, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                       const __grid_constant__ GemmParams p) {
@@ -238,16 +227,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const Schedule& sc = p.sched;
-    const int rank = CL > 1 ? (int)tc::cluster_ctarank() : 0;
-    const int cluster = blockIdx.x / CL, nclusters = gridDim.x / CL;
-    const int num_ctiles = p.num_tiles / CL;
-    constexpr uint16_t kMask = (uint16_t)((1u << CL) - 1);
-    constexpr int A_PART = A_STAGE / CL, A_ROWS = BM / CL;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], CL);  // one commit from every CTA of the cluster
+            tc::mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&accf[b], 1);
@@ -260,9 +244,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
     __syncthreads();
-    // peers multicast into this CTA's shared memory and arrive on its barriers:
-    // every CTA of the cluster must have initialised them first
-    if (CL > 1) tc::cluster_sync();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
@@ -270,9 +251,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (lane == 0) {  // ---------------------------------- TMA producer
             uint32_t it = 0;
             bool ok = true;
-            for (int ct = cluster; ct < num_ctiles && ok; ct += nclusters) {
+            for (int ct = blockIdx.x; ct < p.num_tiles && ok; ct += gridDim.x) {
                 int mb, nb;
-                cluster_tile_coords<CL>(ct, p.num_m_tiles, p.num_n_tiles, rank, mb, nb);
+                tile_coords(ct, p.num_m_tiles, p.num_n_tiles, mb, nb);
                 for (int g = 0; g < sc.n_groups && ok; ++g) {
                     for (int kc = 0; kc < sc.kb_count && ok; kc += KB_CHUNK) {  // same order as the MMA issuer
                         const int kc1 = min(sc.kb_count, kc + KB_CHUNK);
@@ -285,14 +266,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                                     ok = false;
                                     break;
                                 }
-                                // this CTA's own bytes plus the A parts its peers multicast in
                                 tc::mbar_arrive_expect_tx(&full[st], STAGE_BYTES);
                                 uint8_t* sa = smem + st * STAGE_BYTES;
-                                if (CL == 1)
-                                    tc::tma_load_2d(sa, &tmA, kb * BK, arow, &full[st]);
-                                else
-                                    tc::tma_load_2d_multicast(sa + rank * A_PART, &tmA, kb * BK, arow + rank * A_ROWS,
-                                                              &full[st], kMask);
+                                tc::tma_load_2d(sa, &tmA, kb * BK, arow, &full[st]);
                                 tc::tma_load_2d(sa + A_STAGE, &tmB, kb * BK, brow, &full[st]);
                             }
                         }
@@ -308,7 +284,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             constexpr uint32_t ID = tc::idesc(tc::kFmtE4M3, tc::kFmtE4M3, BM, BN);
             uint32_t it = 0, acc_it = 0;
             bool ok = true;
-            for (int ct = cluster; ct < num_ctiles && ok; ct += nclusters) {
+            for (int ct = blockIdx.x; ct < p.num_tiles && ok; ct += gridDim.x) {
                 for (int g = 0; g < sc.n_groups && ok; ++g, ++acc_it) {
                     const uint32_t buf = acc_it & 1;
                     if (!tc::mbar_wait(&acce[buf], ((acc_it >> 1) & 1) ^ 1, p.err, kDevTimeoutAccEmpty)) {
@@ -339,8 +315,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                     tc::mma_f8f6f4(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
                                     accumulate = 1;
                                 }
-                                if (CL == 1) tc::mma_commit(&empty[st]);
-                                else tc::mma_commit_multicast(&empty[st], kMask);
+                                tc::mma_commit(&empty[st]);
                             }
                         }
                     }
@@ -356,17 +331,15 @@ __global__ void __launch_bounds__(THREADS, 1)
         ulonglong2* W = p.W + (size_t)blockIdx.x * (BM * BN);
         const uint64_t pol_keep = tc::policy_evict_last(), pol_stream = tc::policy_evict_first();
         uint32_t acc_it = 0;
-        for (int ct = cluster; ct < num_ctiles; ct += nclusters) {
+        for (int ct = blockIdx.x; ct < p.num_tiles; ct += gridDim.x) {
             int mb, nb;
-            cluster_tile_coords<CL>(ct, p.num_m_tiles, p.num_n_tiles, rank, mb, nb);
+            tile_coords(ct, p.num_m_tiles, p.num_n_tiles, mb, nb);
             if (!epilogue_tile(p, p.sched, mb, nb, tmem, quad, lane, W, accf, acc_it, pol_keep, pol_stream,
                                [&](uint32_t buf) { tc::mbar_arrive(&acce[buf]); }))
                 break;
         }
     }
     __syncthreads();
-    // no CTA leaves while a peer may still multicast into it or arrive on it
-    if (CL > 1) tc::cluster_sync();
     if (warp == 1) {
         __syncwarp();
         tc::tc_fence_after();
@@ -572,15 +545,7 @@ Workspace* workspace(cudaStream_t s) {
     return w;
 }
 
-int num_sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = kNumSMs;
-    }
-    return n;
-}
+int num_sms() { return device_sm_count(); }
 
 // Slice count from the requested accuracy and the measured exponent spread.
 // The fixed-point width F = 4 + 5(S-1) must reach ~1e-15 elementwise
@@ -678,12 +643,9 @@ int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t 
 // Which form of the slice-product GEMM runs, and the padded operand extents
 // it needs.  The CTA-pair form (256 x 256 tiles) runs whenever m spans two or
 // more 128-row tiles and padding m to 256 costs at most ~10% more work; the
-// single-CTA form (128 x 256 tiles) takes the rest, in clusters of CL CTAs
-// along N that share the A slab by multicast: the widest of 4, 2, 1 whose
-// padding of the N tiles costs at most ~10% more work.
+// single-CTA form (128 x 256 tiles) takes the rest.
 struct GemmShape {
     bool pair;
-    int cl;  // cluster width of the single-CTA form (2 for the pair form)
     int64_t m_pad, n_pad;
 };
 
@@ -693,21 +655,8 @@ GemmShape gemm_shape(int64_t m, int64_t n) {
     // COSMA_GPU_OZAKI_PAIR=OFF keeps every GEMM on the single-CTA form
     static const bool pairs = env_bool("COSMA_GPU_OZAKI_PAIR", true);
     g.pair = pairs && mt >= 2 && (mt % 2 == 0 || mt >= 10);
-    if (g.pair) {
-        g.cl = 2;
-        g.m_pad = ceil_div(m, 2 * BM) * 2 * BM;
-        g.n_pad = nt * BN;
-        return g;
-    }
-    g.cl = 1;
-    for (int cl : {4, 2}) {
-        if (nt >= cl && ceil_div(nt, cl) * cl * 10 <= nt * 11) {
-            g.cl = cl;
-            break;
-        }
-    }
-    g.m_pad = mt * BM;
-    g.n_pad = ceil_div(nt, g.cl) * g.cl * BN;
+    g.m_pad = g.pair ? ceil_div(m, 2 * BM) * 2 * BM : mt * BM;
+    g.n_pad = nt * BN;
     return g;
 }
 
@@ -729,24 +678,25 @@ int max_active_clusters(Kernel kern, int cl, int smem, int* out) {
     return COSMA_GPU_SUCCESS;
 }
 
-// Persistent grid: as many whole clusters as fit on the GPU at once (one CTA
-// per SM), but no more than there are cluster tiles.  num_tiles counts CTA
-// tiles for the single-CTA form and 256 x 256 tiles for the pair form.
+// Persistent grid: one CTA per SM (CTA pairs for the pair form), but no more
+// than there are tiles.  num_tiles counts 128 x 256 tiles for the single-CTA
+// form and 256 x 256 tiles for the pair form.
 int gemm_grid(const GemmShape& sh, int num_tiles, int* grid) {
-    static int max_clusters[6] = {0, 0, 0, 0, 0, 0};  // [cl] single-CTA form, [5] pair form
-    const int slot = sh.pair ? 5 : sh.cl;
-    if (!max_clusters[slot]) {
-        int n = 0;
-        if (sh.pair) CGB_CHECK(max_active_clusters(ozaki_gemm_pair_kernel, 2, P_SMEM_BYTES, &n));
-        else if (sh.cl == 1) n = num_sms();
-        else if (sh.cl == 2) CGB_CHECK(max_active_clusters(ozaki_gemm_kernel<2>, 2, SMEM_BYTES, &n));
-        else CGB_CHECK(max_active_clusters(ozaki_gemm_kernel<4>, 4, SMEM_BYTES, &n));
-        n = std::min(n, num_sms() / sh.cl);  // one CTA per SM: never more CTAs than SMs
-        if (n < 1) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki: no cluster of the slice GEMM fits on the GPU");
-        max_clusters[slot] = n;
+    if (!sh.pair) {
+        *grid = std::min(num_tiles, num_sms());
+        return COSMA_GPU_SUCCESS;
     }
-    const int cluster_tiles = sh.pair ? num_tiles : num_tiles / sh.cl;
-    *grid = std::min(cluster_tiles, max_clusters[slot]) * sh.cl;
+    static PerDevice<int> pair_clusters;
+    int n = 0;
+    CGB_CHECK(pair_clusters.get(
+        [](int& v) {
+            CGB_CHECK(max_active_clusters(ozaki_gemm_pair_kernel, 2, P_SMEM_BYTES, &v));
+            v = std::min(v, num_sms() / 2);  // one CTA per SM: never more CTAs than SMs
+            if (v < 1) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki: no CTA pair of the slice GEMM fits on the GPU");
+            return COSMA_GPU_SUCCESS;
+        },
+        &n));
+    *grid = std::min(num_tiles, n) * 2;
     return COSMA_GPU_SUCCESS;
 }
 
@@ -757,46 +707,38 @@ void set_tiles(const GemmShape& sh, GemmParams& p) {
     p.num_tiles = sh.pair ? (p.num_m_tiles / 2) * p.num_n_tiles : p.num_m_tiles * p.num_n_tiles;
 }
 
-template <class Kernel>
-int launch_cluster(Kernel kern, int cl, int grid, int smem, const CUtensorMap& tmA, const CUtensorMap& tmB,
-                   const GemmParams& p, cudaStream_t st) {
-    CGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid, 1, 1);
-    cfg.blockDim = dim3(THREADS, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr;
-    attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = cl;
-    attr.val.clusterDim.y = 1;
-    attr.val.clusterDim.z = 1;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    CGB_CUDA(cudaLaunchKernelEx(&cfg, kern, tmA, tmB, p));
-    return COSMA_GPU_SUCCESS;
-}
-
 // Launches the slice-product GEMM over digit slices laid out [S][rows_pad][k_pad].
 int launch_slice_gemm(const GemmShape& sh, int grid, const void* slicesA, const void* slicesB, int S, int64_t k_pad,
                       const GemmParams& p, cudaStream_t st) {
     CUtensorMap tmA, tmB;
-    // single-CTA clusters: each CTA loads BM/cl rows of the A slab and
-    // multicasts them; pairs: each CTA loads its 128 rows of A and half of B
-    const int a_box = sh.pair ? BM : BM / sh.cl, b_box = sh.pair ? BN / 2 : BN;
+    // pairs: each CTA loads its 128 rows of A and half of the B tile
+    const int a_box = BM, b_box = sh.pair ? BN / 2 : BN;
     CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slicesA, (uint64_t)k_pad,
                            (uint64_t)(S * sh.m_pad), (uint64_t)k_pad, BK, a_box));
     CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, slicesB, (uint64_t)k_pad,
                            (uint64_t)(S * sh.n_pad), (uint64_t)k_pad, BK, b_box));
-    if (sh.pair) return launch_cluster(ozaki_gemm_pair_kernel, 2, grid, P_SMEM_BYTES, tmA, tmB, p, st);
-    if (sh.cl == 1) {
-        CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        ozaki_gemm_kernel<1><<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
-        CGB_CUDA(cudaGetLastError());
+    if (sh.pair) {
+        CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      P_SMEM_BYTES));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid, 1, 1);
+        cfg.blockDim = dim3(THREADS, 1, 1);
+        cfg.dynamicSmemBytes = P_SMEM_BYTES;
+        cfg.stream = st;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = 2;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        CGB_CUDA(cudaLaunchKernelEx(&cfg, ozaki_gemm_pair_kernel, tmA, tmB, p));
         return COSMA_GPU_SUCCESS;
     }
-    if (sh.cl == 2) return launch_cluster(ozaki_gemm_kernel<2>, 2, grid, SMEM_BYTES, tmA, tmB, p, st);
-    return launch_cluster(ozaki_gemm_kernel<4>, 4, grid, SMEM_BYTES, tmA, tmB, p, st);
+    CGB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    ozaki_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
 }
 
 // One call with k <= MAX_K_PER_CALL.
@@ -923,16 +865,11 @@ void split_cplx(int S, bool kcontig, bool bside, const double2* X, int64_t ld, i
 }
 
 // Shape of the complex form: the GEMM has 2*nh columns (real parts, then
-// imaginary parts), nh = n padded to 256; both halves must tile exactly.
+// imaginary parts), nh = n padded to 256, so both halves tile exactly.
 GemmShape cplx_shape(int64_t m, int64_t n, int64_t* nh_out) {
     const int64_t nh = ceil_div(n, BN) * BN;
-    GemmShape sh = gemm_shape(m, 2 * nh);
-    if (sh.n_pad != 2 * nh) {  // 2*nh/256 tiles is even: clusters of 2 tile it exactly
-        sh.cl = 2;
-        sh.n_pad = 2 * nh;
-    }
     *nh_out = nh;
-    return sh;
+    return gemm_shape(m, 2 * nh);
 }
 
 // One complex pass with 2k <= MAX_K_PER_CALL: the same pipeline on the

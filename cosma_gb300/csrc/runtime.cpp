@@ -66,6 +66,23 @@ int default_tile_n() { return (int)env_ll("COSMA_GPU_MAX_TILE_N", 32768); }
 int default_tile_k() { return (int)env_ll("COSMA_GPU_MAX_TILE_K", 32768); }
 bool default_pinning() { return env_bool("COSMA_GPU_MEMORY_PINNING", true); }
 
+int device_sm_count() {
+    static PerDevice<int> cache;
+    int n = kNumSMs;
+    if (cache.get(
+            [](int& v) {
+                int dev = 0;
+                if (cudaGetDevice(&dev) != cudaSuccess ||
+                    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+                    v = kNumSMs;
+                cudaGetLastError();
+                return 0;
+            },
+            &n) != 0)
+        n = kNumSMs;
+    return n;
+}
+
 int default_method() {
     const char* v = env_raw("COSMA_GPU_GEMM_METHOD");
     if (!v) return COSMA_GPU_METHOD_AUTO;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 
 struct cosma_gpu_oz_grouped_plan;  // grouped Ozaki plan (ozaki_grouped.cu)
 
@@ -18,6 +19,47 @@ int default_tile_n();
 int default_tile_k();
 bool default_pinning();
 int default_method();
+
+// A value computed once per device (an occupancy figure, an SM count, a
+// kernel attribute having been set) and cached for the process lifetime.
+// Threads that ask for the same device at the same time compute it once; a
+// computation that fails is retried by the next caller.
+template <class T>
+class PerDevice {
+   public:
+    static constexpr int kMaxDevices = 64;
+    // compute(T&) returns a status; on success the value is cached for the
+    // current device and copied to *out.
+    template <class F>
+    int get(F&& compute, T* out) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = kMaxDevices;
+        std::lock_guard<std::mutex> lock(mu_);
+        if (dev == kMaxDevices) {  // beyond the table: no caching
+            T v{};
+            const int s = compute(v);
+            if (s == 0) *out = v;
+            return s;
+        }
+        if (!have_[dev]) {
+            T v{};
+            const int s = compute(v);
+            if (s != 0) return s;
+            val_[dev] = v;
+            have_[dev] = true;
+        }
+        *out = val_[dev];
+        return 0;
+    }
+
+   private:
+    std::mutex mu_;
+    bool have_[kMaxDevices] = {};
+    T val_[kMaxDevices] = {};
+};
+
+// SM count of the current device (cached per device; 152 if the query fails).
+int device_sm_count();
 
 // Scalar kinds of the four GEMM flavours.
 enum class Scalar { S, D, C, Z };

@@ -85,18 +85,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// 2-D TMA tile load multicast to every CTA of the cluster in `mask`: the
-// tile lands at the same shared-memory offset in each of them and completes
-// the transaction on the mbarrier at the same offset in each of them.
-__device__ __forceinline__ void tma_load_2d_multicast(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
-                                                      uint16_t mask) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3}], [%4], %5;"
-        ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
-        : "memory");
-}
-
 // ----------------------------------------------------------- CTA pairs
 // A pair of CTAs (cluster of 2) running one tcgen05.mma.cta_group::2: the
 // even CTA issues the MMAs, each CTA holds half of every operand tile and
@@ -223,13 +211,6 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_
 // Arrives on `bar` once every tcgen05.mma issued so far by this thread has completed.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-// Same, arriving on the mbarrier at the same offset in every CTA of `mask`.
-__device__ __forceinline__ void mma_commit_multicast(uint64_t* bar, uint16_t mask) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-                 ::"r"(smem_u32(bar)), "h"(mask)
                  : "memory");
 }
 

@@ -194,15 +194,20 @@ int cosma_gpu_zgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n,
  * library allocate device memory: applications whose device memory is all
  * owned by their own pool allocator, and code that must not trigger the
  * device-wide synchronisation cudaMalloc / cudaFree imply.  Arguments and
- * results are those of cosma_gpu_dgemm_ozaki_device (same kernels, same
- * output bits); the caller still provides A, B and C in device memory.
+ * C are those of cosma_gpu_dgemm_ozaki_device (same kernels, same output
+ * bits); the caller still provides A, B and C in device memory.  In *info
+ * the slice fields and fallback_native are filled, prep_ms and gemm_ms stay
+ * 0 (this entry point creates no timing events).
  * Scratch comes from one static device array of
  * COSMA_GPU_OZAKI_NOALLOC_SCRATCH_BYTES; problems needing more are rejected
  * with COSMA_GPU_ERROR_INVALID_ARGUMENT and a message giving the size (about
  * m = n = k = 1024 with 13 slices fits).  The first call on each device looks
- * up the array's device address, so make it before any stream capture.  All
- * calls share the one array: calls that overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller. */
+ * up the array's device address, so make it before any stream capture.  Each
+ * call waits for its stream twice per pass over K (k beyond 65536 takes
+ * several passes): once to read the exponent statistics that fix the slice
+ * count, once to read the kernels' error word.  All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller. */
 int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m, int64_t n, int64_t k,
                                   double alpha, const double* A, int64_t lda, const double* B,
                                   int64_t ldb, double beta, double* C, int64_t ldc, int slices,

@@ -56,6 +56,40 @@ def test_no_alloc_matches_allocating_entry_point_on_consecutive_calls(native_lib
             np.testing.assert_array_equal(from_dev(got, m, n), from_dev(ref, m, n))
 
 
+def test_no_alloc_multi_pass_k_and_nan_fallback(native_lib, cuda):
+    """k beyond one exact pass (65536) runs as two passes accumulated through C
+    (beta becomes 1 after the first), and an operand holding NaN falls back to
+    the native kernel; both paths differ in code from the allocating twin, so
+    both are compared bit for bit against it, twice in a row."""
+    lib = native_lib
+    # 2 slices keep the 65536-deep pass inside the static array: 2 x (128 + 256) x 65536 bytes
+    m, n, k, slices = 72, 40, 65536 + 64, 2
+    A = oracle.uniform((m, k), 11)
+    B = oracle.uniform((k, n), 12)
+    C0 = oracle.uniform((m, n), 13)
+    nanA = A[:, :200].copy()
+    nanA[5, 17] = np.nan
+    cases = [(A, B, k, False), (nanA, B[:200].copy(), 200, True)]
+    for a, b, kk, fallback in cases:
+        dA, dB = to_dev(a), to_dev(b)
+        ref = to_dev(C0)
+        st, ref_info = _call(lib.cosma_gpu_dgemm_ozaki_device, "N", "N", m, n, kk, dA, m, dB, kk, ref, m, slices,
+                             alpha=0.75, beta=2.0)
+        assert st == 0, lib.cosma_gpu_last_error_string()
+        assert ref_info.fallback_native == int(fallback)
+        want = from_dev(ref, m, n)
+        if fallback:
+            assert np.isnan(want[5]).all() and not np.isnan(np.delete(want, 5, axis=0)).any()
+        for _ in range(2):
+            got = to_dev(C0)
+            st, info = _call(lib.cosma_gpu_dgemm_ozaki_noalloc, "N", "N", m, n, kk, dA, m, dB, kk, got, m, slices,
+                             alpha=0.75, beta=2.0)
+            assert st == 0, lib.cosma_gpu_last_error_string()
+            assert info.fallback_native == int(fallback)
+            assert info.prep_ms == 0.0 and info.gemm_ms == 0.0  # documented: no timing events here
+            np.testing.assert_array_equal(from_dev(got, m, n), want)
+
+
 def test_no_alloc_rejects_problems_beyond_its_scratch(native_lib, cuda):
     import torch
     lib = native_lib
