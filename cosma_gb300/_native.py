@@ -12,8 +12,9 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libcosma_gb300.so"
 
 SUCCESS = 0
-METHOD_AUTO, METHOD_NATIVE, METHOD_OZAKI, METHOD_BF16X3 = 0, 1, 2, 3
-METHODS = {"auto": METHOD_AUTO, "native": METHOD_NATIVE, "ozaki": METHOD_OZAKI, "bf16x3": METHOD_BF16X3}
+METHOD_AUTO, METHOD_NATIVE, METHOD_OZAKI, METHOD_BF16X3, METHOD_OZAKI2 = 0, 1, 2, 3, 4
+METHODS = {"auto": METHOD_AUTO, "native": METHOD_NATIVE, "ozaki": METHOD_OZAKI, "bf16x3": METHOD_BF16X3,
+           "ozaki2": METHOD_OZAKI2}
 
 
 class CosmaGpuError(RuntimeError):
@@ -24,7 +25,8 @@ class CosmaGpuError(RuntimeError):
 
 class OzakiInfo(C.Structure):
     _fields_ = [("slices", C.c_int), ("products", C.c_int), ("groups", C.c_int), ("fallback_native", C.c_int),
-                ("spread_bits", C.c_double), ("prep_ms", C.c_double), ("gemm_ms", C.c_double)]
+                ("spread_bits", C.c_double), ("prep_ms", C.c_double), ("gemm_ms", C.c_double),
+                ("fraction_bits", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -98,6 +100,11 @@ SIGNATURES = {
                                            C.POINTER(OzakiInfo)]),
     "cosma_gpu_zgemm_ozaki_device": (i32, [ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, i32, vp,
                                            C.POINTER(OzakiInfo)]),
+    "cosma_gpu_dgemm_ozaki2_device": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
+                                            C.POINTER(OzakiInfo)]),
+    "cosma_gpu_zgemm_ozaki2_device": (i32, [ch, ch, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, i32, vp,
+                                            C.POINTER(OzakiInfo)]),
+    "cosma_gpu_ozaki2_choose": (i32, [i64, dbl, i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cosma_gpu_dgemm_ozaki_noalloc": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                             C.POINTER(OzakiInfo)]),
     "cosma_gpu_grouped_plan_create": (vp, [i32, i32, C.POINTER(GemmProblem), i32, vp]),

@@ -249,6 +249,35 @@ def zgemm_ozaki_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm,
     return info.as_dict()
 
 
+def dgemm_ozaki2_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc, moduli=0, stream=None):
+    """FP64-accurate DGEMM by the Chinese-remainder (Ozaki scheme II) form on
+    CUDA buffers; returns the statistics (slices = modulus count,
+    fraction_bits = P)."""
+    lib = N.load()
+    info = N.OzakiInfo()
+    N.check(lib.cosma_gpu_dgemm_ozaki2_device(transa.encode(), transb.encode(), m, n, k, alpha, ptr(A), lda, ptr(B),
+                                              ldb, beta, ptr(Cm), ldc, moduli, _stream_ptr(stream), C.byref(info)))
+    return info.as_dict()
+
+
+def zgemm_ozaki2_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc, moduli=0, stream=None):
+    """The Chinese-remainder form for complex128 CUDA buffers (op N/T/C)."""
+    lib = N.load()
+    info = N.OzakiInfo()
+    al, be = _cplx_pair(alpha, C.c_double), _cplx_pair(beta, C.c_double)
+    N.check(lib.cosma_gpu_zgemm_ozaki2_device(transa.encode(), transb.encode(), m, n, k, al, ptr(A), lda, ptr(B),
+                                              ldb, be, ptr(Cm), ldc, moduli, _stream_ptr(stream), C.byref(info)))
+    return info.as_dict()
+
+
+def ozaki2_choose(k, spread_bits=0.0, moduli=0):
+    """(modulus count, fraction bits P) the Chinese-remainder form uses (host only)."""
+    lib = N.load()
+    nm, P = C.c_int(), C.c_int()
+    N.check(lib.cosma_gpu_ozaki2_choose(int(k), float(spread_bits), int(moduli), C.byref(nm), C.byref(P)))
+    return nm.value, P.value
+
+
 class BlockLayout:
     """A matrix described block by block, as the reference's C `layout`:
     block (r, c) covers rows rowsplit[r]:rowsplit[r+1] and columns

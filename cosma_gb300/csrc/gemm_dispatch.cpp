@@ -29,7 +29,7 @@ void DeviceBuffer::release() {
 static bool is_zero(const double* v, Scalar s) { return v[0] == 0.0 && (!scalar_complex(s) || v[1] == 0.0); }
 
 int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
     if (g.m < 0 || g.n < 0 || g.k < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: negative size");
     if (g.opa < 0 || g.opb < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: op must be N, T or C");
     if (g.m == 0 || g.n == 0) return COSMA_GPU_SUCCESS;
@@ -43,9 +43,12 @@ int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t st
     // native kernel uses for FP32 inputs is ~60x slower on GB300).
     if (method == COSMA_GPU_METHOD_AUTO)
         method = g.scalar == Scalar::S ? COSMA_GPU_METHOD_BF16X3 : COSMA_GPU_METHOD_NATIVE;
-    if (method == COSMA_GPU_METHOD_OZAKI) {
-        if (g.scalar == Scalar::D) return ozaki_dgemm(g, ozaki_slices, stream, info);
-        if (g.scalar == Scalar::Z) return ozaki_zgemm(g, ozaki_slices, stream, info);
+    if (method == COSMA_GPU_METHOD_OZAKI || method == COSMA_GPU_METHOD_OZAKI2) {
+        const bool crt = method == COSMA_GPU_METHOD_OZAKI2;
+        if (g.scalar == Scalar::D)
+            return crt ? ozaki2_dgemm(g, ozaki_slices, stream, info) : ozaki_dgemm(g, ozaki_slices, stream, info);
+        if (g.scalar == Scalar::Z)
+            return crt ? ozaki2_zgemm(g, ozaki_slices, stream, info) : ozaki_zgemm(g, ozaki_slices, stream, info);
         // single precision: the tensor-core form accurate to FP32 (real), or
         // the native kernel (complex), so that a process-wide Ozaki default
         // also serves psgemm / pcgemm callers
@@ -126,6 +129,23 @@ int cosma_gpu_dgemm_ozaki_device(char ta, char tb, int64_t m, int64_t n, int64_t
     double a[2] = {alpha, 0}, b[2] = {beta, 0};
     auto g = cgb::make_desc(cgb::Scalar::D, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc);
     return cgb::gemm_device(g, COSMA_GPU_METHOD_OZAKI, slices, (cudaStream_t)stream, info);
+}
+
+int cosma_gpu_dgemm_ozaki2_device(char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+                                  int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                                  int moduli, void* stream, cosma_gpu_ozaki_info* info) {
+    cgb::clear_error();
+    double a[2] = {alpha, 0}, b[2] = {beta, 0};
+    auto g = cgb::make_desc(cgb::Scalar::D, ta, tb, m, n, k, a, A, lda, B, ldb, b, C, ldc);
+    return cgb::gemm_device(g, COSMA_GPU_METHOD_OZAKI2, moduli, (cudaStream_t)stream, info);
+}
+
+int cosma_gpu_zgemm_ozaki2_device(char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,
+                                  const double* A, int64_t lda, const double* B, int64_t ldb, const double* beta,
+                                  double* C, int64_t ldc, int moduli, void* stream, cosma_gpu_ozaki_info* info) {
+    cgb::clear_error();
+    auto g = cgb::make_desc(cgb::Scalar::Z, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    return cgb::gemm_device(g, COSMA_GPU_METHOD_OZAKI2, moduli, (cudaStream_t)stream, info);
 }
 
 int cosma_gpu_zgemm_ozaki_device(char ta, char tb, int64_t m, int64_t n, int64_t k, const double* alpha,

@@ -555,9 +555,13 @@ int num_sms() { return device_sm_count(); }
 // longer K needs fewer (the truncation errors average out against a C that
 // grows with k), and 60 bits are the floor for well-scaled data; 3 bits of
 // margin cover the worst-conditioned entries of larger samples.
-int choose_slices(double spread_bits, int64_t k) {
+double required_fraction_bits(double spread_bits, int64_t k) {
     const double lk = std::log2((double)std::max<int64_t>(k, 1));
-    const double F = std::max(60.0, 65.0 + 0.85 * (spread_bits - 3.3) - (lk - 8.0));
+    return std::max(60.0, 65.0 + 0.85 * (spread_bits - 3.3) - (lk - 8.0));
+}
+
+int choose_slices(double spread_bits, int64_t k) {
+    const double F = required_fraction_bits(spread_bits, k);
     int S = (int)std::ceil((F - 4.0) / 5.0) + 1;
     return std::min(std::max(S, 2), MAX_SLICES);
 }
@@ -616,8 +620,8 @@ void split(int S, bool kcontig, const double* X, int64_t ld, int64_t rows, int64
 // Row scaling of a (rows x k) operand; kcontig as in split_kernel.  es = 2
 // for complex operands (ld in complex elements): a row's exponent covers the
 // real and imaginary parts, and the spread is measured over 2k terms.
-int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, int* exps, Workspace* w,
-               Stats* st_dev, int which, cudaStream_t st, int es = 1) {
+int scale_operand(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, int* exps, DeviceBuffer& part,
+                  Stats* st_dev, int which, cudaStream_t st, int es) {
     if (rows == 0) return COSMA_GPU_SUCCESS;
     if (kcontig) {
         // a complex row is 2k consecutive doubles
@@ -628,9 +632,9 @@ int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t 
         int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
         nchunks = (int)std::min<int64_t>(nchunks, std::max<int64_t>(1, k / 64));
         const int64_t kchunk = ceil_div(k, nchunks);
-        CGB_CHECK(w->part.reserve((size_t)nchunks * rows * 8, st));
-        int* pe = (int*)w->part.ptr;
-        float* pm = (float*)((char*)w->part.ptr + (size_t)nchunks * rows * 4);
+        CGB_CHECK(part.reserve((size_t)nchunks * rows * 8, st));
+        int* pe = (int*)part.ptr;
+        float* pm = (float*)((char*)part.ptr + (size_t)nchunks * rows * 4);
         scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
             X, ld * es, es, rows, k, kchunk, pe, pm, st_dev);
         scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, rows, k * es, exps,
@@ -638,6 +642,11 @@ int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t 
     }
     CGB_CUDA(cudaGetLastError());
     return COSMA_GPU_SUCCESS;
+}
+
+int scale_rows(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, int* exps, Workspace* w,
+               Stats* st_dev, int which, cudaStream_t st, int es = 1) {
+    return scale_operand(kcontig, X, ld, rows, k, exps, w->part, st_dev, which, st, es);
 }
 
 // Which form of the slice-product GEMM runs, and the padded operand extents
@@ -824,6 +833,7 @@ int ozaki_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki_
         cudaEventElapsedTime(&prep, w->ev[0], w->ev[1]);
         cudaEventElapsedTime(&gemm, w->ev[2], w->ev[3]);
         info->slices = S;
+        info->fraction_bits = 4 + 5 * (S - 1);
         info->products = products;
         info->groups = p.sched.n_groups;
         info->spread_bits = spread;
@@ -970,6 +980,7 @@ int ozaki_zchunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki
         cudaEventElapsedTime(&prep, w->ev[0], w->ev[1]);
         cudaEventElapsedTime(&gemm, w->ev[2], w->ev[3]);
         info->slices = S;
+        info->fraction_bits = 4 + 5 * (S - 1);
         info->products = products;
         info->groups = p.sched.n_groups;
         info->spread_bits = spread;
@@ -987,7 +998,7 @@ int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: buffers must be 8-byte aligned");
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: m and n are limited to 2^24");
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
     // K beyond one exact accumulator pass is cut into chunks accumulated
     // through C (beta = 1 after the first chunk).
     GemmDesc c = g;
@@ -1008,7 +1019,7 @@ int ozaki_zgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: complex buffers must be 16-byte aligned");
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 23)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: m is limited to 2^24 and n to 2^23 (complex)");
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
     // each complex term is two real terms: half the real pass length per chunk
     const int64_t kmax = oz::MAX_K_PER_CALL / 2;
     GemmDesc c = g;
@@ -1209,6 +1220,7 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
         int products = 0;
         for (int i = 0; i < p.sched.n_groups; ++i) products += p.sched.gcount[i];
         info->slices = S;
+        info->fraction_bits = 4 + 5 * (S - 1);
         info->products = products;
         info->groups = p.sched.n_groups;
         info->spread_bits = spread;
@@ -1225,7 +1237,7 @@ extern "C" int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m
                                              cosma_gpu_ozaki_info* info) {
     using namespace cgb;
     clear_error();
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
     const int opa = parse_op(transa), opb = parse_op(transb);
     if (opa < 0 || opb < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: op must be N, T or C");
     if (m < 0 || n < 0 || k < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: negative size");

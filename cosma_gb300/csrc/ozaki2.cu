@@ -1,0 +1,1125 @@
+// FP64-accurate GEMM by the Chinese-remainder form of the Ozaki scheme
+// ("Ozaki scheme II", Ozaki, Uchino & Imamura 2025) on the BF16 tensor cores.
+//
+// The reference runs a native DGEMM (cuBLAS through Tiled-MM); this is a
+// precision form of the same operation, C = alpha*op(A)*op(B) + beta*C, next
+// to the digit-slice form of ozaki.cu.  It needs one GEMM per modulus where
+// the slice form needs S(S+1)/2 slice products, which is what makes it the
+// faster of the two at FP64 accuracy.
+//
+// Method:
+//  1. Row scaling (shared with the slice form): row i of op(A) gets the
+//     exponent E_i = 1 + floor(log2 max_l |a_il|), column j of op(B) F_j.
+//  2. Integers.  a'_il = sign(a) round_half_away(|a_il| 2^(P - E_i)), an
+//     integer of at most P bits; b'_lj likewise.  P is the fraction width,
+//     chosen from the requested accuracy and the exponent spread.
+//  3. Residues.  For N pairwise coprime moduli p_t <= 255 (product M >
+//     4 k 2^(2P)), the balanced residues of a' and b' modulo p_t lie in
+//     [-127, 127] and are exact in BF16; they are written as N BF16 matrices
+//     per operand, K-major.
+//  4. Modular GEMMs.  For each t, A_t * B_t runs on the BF16 tensor cores
+//     (tcgen05 kind::f16, CTA pairs, TMA).  One TMEM accumulation spans a
+//     1024-wide K chunk: 1024 products of magnitude <= 127^2 sum below 2^24,
+//     so the FP32 accumulator is exact.  The epilogue adds each chunk, as an
+//     integer, into 32-bit running sums in registers and finally reduces them
+//     modulo p_t: one residue byte per output and modulus.
+//  5. Reconstruction.  V_ij = sum_t r_t w_t mod M (w_t the CRT weights), taken
+//     in (-M/2, M/2), is exactly sum_l a'_il b'_lj; it is rounded once to FP64
+//     with the scale 2^(E_i + F_j - 2P) (round to nearest even), then alpha
+//     and beta are applied.  The integer arithmetic is 32-bit limbs; no FP64
+//     arithmetic is used before the final conversion.
+//
+// The integer tensor op (tcgen05 kind::i8) does not exist on sm_103a and FP8
+// E4M3 holds integers only up to 16, too few pairwise coprime moduli for
+// FP64 accuracy; BF16 holds all integers up to 256.
+//
+// GEMM kernel: persistent CTA pairs, 256 x 256 output tiles (M = 256 over the
+// pair), 64-element (128-byte) BF16 K blocks through a 4-stage TMA ring with
+// 128-byte swizzle, two 256-column FP32 accumulators in TMEM so that the
+// drain of one K chunk overlaps the MMAs of the next.  Work units are
+// (modulus, tile) pairs, modulus-major: at any time the wave of CTAs runs
+// one ordinary BF16 GEMM, whose operand panels it shares through L2.
+//   warp 0      TMA producer         warp 1   TMEM owner + MMA issuer
+//   warps 2..9  epilogue (TMEM -> registers -> 32-bit running sums)
+#include "common.cuh"
+#include "runtime.hpp"
+#include "ozaki_common.cuh"
+#include "tc_common.cuh"
+#include "tma_host.hpp"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+
+namespace cgb {
+namespace oz2 {
+
+using oz::Stats;
+
+constexpr int MAX_MODULI = 28;
+// Pairwise coprime, largest first: 255 = 3*5*17, 254 = 2*127, 253 = 11*23,
+// 247 = 13*19, the rest primes.
+constexpr uint32_t kModuli[MAX_MODULI] = {255, 254, 253, 251, 247, 241, 239, 233, 229, 227, 223, 211, 199, 197,
+                                          193, 191, 181, 179, 173, 167, 163, 157, 151, 149, 139, 137, 131, 113};
+constexpr int LIMBS = 8;  // 32-bit limbs of the reconstruction (M < 2^214, sums < 2^227)
+
+constexpr int BM = 128, BN = 256, BKE = 64;  // BKE: BF16 elements per K block (128 bytes)
+constexpr int KB_PER_CHUNK = 16;             // 1024-element K chunk per exact TMEM accumulation
+constexpr int CHUNKS_PER_REDUCE = 64;        // running sums reduced mod p after this many chunks
+constexpr int STAGES = 4;
+constexpr int A_STAGE = BM * 128, B_STAGE = (BN / 2) * 128, STAGE = A_STAGE + B_STAGE;  // per CTA
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
+constexpr int SMEM_BYTES = STAGES * STAGE + 1024 + 256;
+static_assert(SMEM_BYTES <= 232448, "shared memory");
+constexpr int kStripPairs = 8;  // tile order: strips of 8 pair rows (2048 rows), see oz::tile_coords
+constexpr int64_t KMAX = 64 * 65535;  // K of one exact pass: the split grids' K extent
+
+// ------------------------------------------------------------ modular helpers
+// u mod p for u < 2^32, magic = floor(2^32 / p): the quotient estimate
+// umulhi(u, magic) is floor(u/p) or one less, so one correction suffices.
+__device__ __forceinline__ uint32_t mod32(uint32_t u, uint32_t p, uint32_t magic) {
+    const uint32_t q = __umulhi(u, magic);
+    const uint32_t r = u - q * p;
+    return r >= p ? r - p : r;
+}
+
+struct SplitParams {
+    int nmod;
+    int P;  // fraction bits
+    uint32_t p[MAX_MODULI], magic[MAX_MODULI], c32[MAX_MODULI];  // c32 = 2^32 mod p
+};
+
+struct RowInt {  // |x| 2^(P - E) rounded = (mhi:mlo) * 2^sh, 0 <= sh < 128
+    uint32_t mlo, mhi;
+    int sh;
+    bool neg;
+};
+
+__device__ __forceinline__ RowInt scaled_integer(double x, int E, int P) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    RowInt v;
+    v.neg = (b >> 63) != 0;
+    const int ef = (int)((b >> 52) & 0x7FF);
+    unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+    int eu;
+    if (ef == 0) eu = -1074; else { M |= 1ull << 52; eu = ef - 1075; }
+    int sh = eu - E + P;
+    if (M == 0) sh = 0;
+    if (sh < 0) {  // round half away from zero
+        const int r = -sh;
+        M = r > 63 ? 0ull : (M + (1ull << (r - 1))) >> r;
+        sh = 0;
+    }
+    v.mlo = (uint32_t)M;
+    v.mhi = (uint32_t)(M >> 32);
+    v.sh = sh;
+    return v;
+}
+
+// Balanced residue of the scaled integer modulo p: in [-(p-1)/2, p/2] (p odd),
+// [-126, 127] for p = 254.
+__device__ __forceinline__ int balanced_residue(const RowInt& v, uint32_t p, uint32_t magic, uint32_t c32,
+                                                uint32_t pow2) {
+    uint32_t r = mod32(v.mlo, p, magic);
+    r = mod32(v.mhi * c32 + r, p, magic);  // mhi < 2^21, c32 < 2^8
+    r = mod32(r * pow2, p, magic);         // < 2^16
+    int s = (int)r;
+    if (s > (int)(p >> 1)) s -= (int)p;
+    return v.neg ? -s : s;
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(int v) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)v));
+}
+
+// 2^s mod p for s < 128 and every modulus, in shared memory.
+__device__ __forceinline__ void fill_pow2(uint8_t (*pow2)[128], const SplitParams& sp) {
+    for (int idx = threadIdx.x; idx < sp.nmod * 128; idx += blockDim.x) {
+        const int t = idx >> 7, s = idx & 127;
+        const uint32_t p = sp.p[t], mg = sp.magic[t];
+        uint32_t r = 1 % p, base = 2 % p;
+        for (int e = s; e; e >>= 1) {
+            if (e & 1) r = mod32(r * base, p, mg);
+            base = mod32(base * base, p, mg);
+        }
+        pow2[t][s] = (uint8_t)r;
+    }
+}
+
+// Residue matrices of a real (rows x k) operand: N BF16 matrices [t][rows_pad][k_pad],
+// zero padded.  A block of 256 threads covers 32 rows x 64 K elements, each
+// thread 8 consecutive K elements of one row (one 16-byte store per modulus).
+// kcontig: element (r, l) at X[l + r*ld], else at X[r + l*ld].
+template <bool KCONTIG>
+__global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows,
+                                                    int64_t k, const int* __restrict__ exps, int64_t k_pad,
+                                                    int64_t rows_pad, uint16_t* __restrict__ out,
+                                                    const __grid_constant__ SplitParams sp) {
+    __shared__ uint8_t pow2[MAX_MODULI][128];
+    fill_pow2(pow2, sp);
+    __syncthreads();
+    const int t = threadIdx.x;
+    int64_t r;
+    int kc;
+    if (KCONTIG) { r = (int64_t)blockIdx.x * 32 + t / 8; kc = t % 8; }
+    else { r = (int64_t)blockIdx.x * 32 + t % 32; kc = t / 32; }
+    const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 8;
+    if (r >= rows_pad || l0 >= k_pad) return;
+    const int E = r < rows ? exps[r] : 0;
+    RowInt v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int64_t l = l0 + e;
+        double x = 0.0;
+        if (r < rows && l < k) x = KCONTIG ? X[l + r * ld] : X[r + l * ld];
+        v[e] = scaled_integer(x, E, sp.P);
+    }
+    uint16_t* o = out + r * k_pad + l0;
+    const int64_t slab = rows_pad * k_pad;
+#pragma unroll 1
+    for (int m = 0; m < sp.nmod; ++m) {
+        const uint32_t p = sp.p[m], mg = sp.magic[m], c = sp.c32[m];
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+            const uint32_t lo = bf16_bits(balanced_residue(v[e], p, mg, c, pow2[m][v[e].sh]));
+            const uint32_t hi = bf16_bits(balanced_residue(v[e + 1], p, mg, c, pow2[m][v[e + 1].sh]));
+            w[e / 2] = lo | (hi << 16);
+        }
+        *reinterpret_cast<uint4*>(o + m * slab) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// Complex operands, laid out like the slice form's complex split: one real
+// GEMM of depth 2*kh gives both parts of C,
+//   A_cat row r                 [ Re a | sa*Im a ]
+//   B_cat row r                 [ Re b | -sb*Im b ]   -> Re C column r
+//   B_cat row rows_pad + r      [ sb*Im b | Re b ]    -> Im C column r
+// (sa, sb = -1 for a conjugated operand).  A negated residue is the residue
+// of the negated integer, so the signs are applied to the residues.  kh is k
+// padded to 64; the row pitch is 2*kh; modulus t starts at t * slice_rows *
+// 2*kh.  X holds interleaved complex doubles, ld in complex elements.
+template <bool KCONTIG, bool BSIDE>
+__global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restrict__ X, int64_t ld, int64_t rows,
+                                                         int64_t k, const int* __restrict__ exps, int64_t kh,
+                                                         int64_t rows_pad, int64_t slice_rows, int conj,
+                                                         uint16_t* __restrict__ out,
+                                                         const __grid_constant__ SplitParams sp) {
+    __shared__ uint8_t pow2[MAX_MODULI][128];
+    fill_pow2(pow2, sp);
+    __syncthreads();
+    const int t = threadIdx.x;
+    int64_t r;
+    int kc;
+    if (KCONTIG) { r = (int64_t)blockIdx.x * 32 + t / 8; kc = t % 8; }
+    else { r = (int64_t)blockIdx.x * 32 + t % 32; kc = t / 32; }
+    const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 8;
+    if (r >= rows_pad || l0 >= kh) return;
+    const int E = r < rows ? exps[r] : 0;
+    const int64_t pitch = 2 * kh, slab = slice_rows * pitch;
+    const double* Xd = reinterpret_cast<const double*>(X);
+#pragma unroll 1
+    for (int part = 0; part < 2; ++part) {
+        RowInt v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int64_t l = l0 + e;
+            double x = 0.0;
+            if (r < rows && l < k) x = Xd[2 * (KCONTIG ? l + r * ld : r + l * ld) + part];
+            v[e] = scaled_integer(x, E, sp.P);
+            if (part && conj) v[e].neg = !v[e].neg;  // the conjugated imaginary part
+        }
+#pragma unroll 1
+        for (int m = 0; m < sp.nmod; ++m) {
+            const uint32_t p = sp.p[m], mg = sp.magic[m], c = sp.c32[m];
+            uint32_t w[4], nw[4];
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+                const int a = balanced_residue(v[e], p, mg, c, pow2[m][v[e].sh]);
+                const int b = balanced_residue(v[e + 1], p, mg, c, pow2[m][v[e + 1].sh]);
+                w[e / 2] = bf16_bits(a) | (bf16_bits(b) << 16);
+                nw[e / 2] = bf16_bits(-a) | (bf16_bits(-b) << 16);
+            }
+            uint16_t* base = out + m * slab;
+            const uint4 val = make_uint4(w[0], w[1], w[2], w[3]);
+            if (!BSIDE) {
+                *reinterpret_cast<uint4*>(base + r * pitch + part * kh + l0) = val;
+            } else if (part == 0) {  // Re b: first half of row r, second half of row rows_pad + r
+                *reinterpret_cast<uint4*>(base + r * pitch + l0) = val;
+                *reinterpret_cast<uint4*>(base + (rows_pad + r) * pitch + kh + l0) = val;
+            } else {  // Im b: negated in row r, as is in row rows_pad + r
+                *reinterpret_cast<uint4*>(base + r * pitch + kh + l0) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+                *reinterpret_cast<uint4*>(base + (rows_pad + r) * pitch + l0) = val;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ GEMM
+struct GemmParams {
+    int num_m_tiles, num_n_tiles, num_tiles;  // 128-row / 256-column tiles; num_tiles counts 256 x 256
+    int nmod, kb_count;
+    int a_rows_pad, b_rows_pad;  // rows of one modulus' residue matrix
+    int64_t m_pad, nb16;         // residue output: [t][n_pad / 16][m_pad][16] bytes
+    uint8_t* R;
+    uint32_t p[MAX_MODULI], magic[MAX_MODULI], bias[MAX_MODULI];  // bias: a multiple of p >= 2^30
+    unsigned* err;
+};
+
+// Reduces the 32 running sums of one column group to residues in [0, p).
+__device__ __forceinline__ void reduce_sums(int (&s)[32], uint32_t p, uint32_t magic, uint32_t bias) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) s[j] = (int)mod32((uint32_t)s[j] + bias, p, magic);  // s + bias in [0, 2^32)
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    gemm_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const __grid_constant__ GemmParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* full = (uint64_t*)(smem + STAGES * STAGE);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf = empty + STAGES;
+    uint64_t* acce = accf + 2;
+    uint64_t* drain = acce + 2;
+    uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rank = (int)tc::cluster_ctarank();
+    const bool leader = rank == 0;
+    const int pair = blockIdx.x / 2, npairs = gridDim.x / 2;
+    const int num_pm = p.num_m_tiles / 2;  // 256-row tiles
+    const int units = p.nmod * p.num_tiles;
+    const int nchunks = (p.kb_count + KB_PER_CHUNK - 1) / KB_PER_CHUNK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            tc::mbar_init(&full[s], 1);   // the even CTA's expect_tx (bytes of both CTAs)
+            tc::mbar_init(&empty[s], 1);  // one MMA commit per use
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&accf[b], 1);
+            tc::mbar_init(&acce[b], 2 * EPI_WARPS);  // every epilogue warp of both CTAs
+        }
+        tc::mbar_init(drain, 1);
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) tc::tmem_alloc_pair(tmem_slot, 512);
+    __syncthreads();
+    tc::cluster_sync();  // the peer's loads and commits reach this CTA's barriers
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---------------------------------- TMA producer (both CTAs)
+            const uint32_t full0 = tc::mapa_shared(full, 0);
+            uint32_t it = 0;
+            bool ok = true;
+            for (int u = pair; u < units && ok; u += npairs) {
+                const int t = u / p.num_tiles, tile = u - t * p.num_tiles;
+                int mbp, nb;
+                oz::tile_coords(tile, num_pm, p.num_n_tiles, mbp, nb, kStripPairs);
+                const int arow = t * p.a_rows_pad + (2 * mbp + rank) * BM;
+                const int brow = t * p.b_rows_pad + nb * BN + rank * (BN / 2);
+                for (int kb = 0; kb < p.kb_count; ++kb, ++it) {
+                    const int st = it % STAGES;
+                    if (!tc::mbar_wait(&empty[st], ((it / STAGES) & 1) ^ 1, p.err, kDevTimeoutEmpty)) {
+                        ok = false;
+                        break;
+                    }
+                    if (leader) tc::mbar_arrive_expect_tx(&full[st], 2 * STAGE);
+                    uint8_t* sa = smem + st * STAGE;
+                    tc::tma_load_2d_pair(sa, &tmA, kb * BKE, arow, full0 + st * 8);
+                    tc::tma_load_2d_pair(sa + A_STAGE, &tmB, kb * BKE, brow, full0 + st * 8);
+                }
+            }
+            if (leader) {  // nothing may still be in flight into either CTA when it exits
+                const uint32_t first = it > STAGES ? it - STAGES : 0;
+                for (uint32_t j = first; j < it; ++j) tc::mbar_wait_drain(&full[j % STAGES], (j / STAGES) & 1);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0 && leader) {  // ------------------------ MMA issuer (even CTA)
+            constexpr uint32_t ID = tc::idesc(tc::kFmtBF16, tc::kFmtBF16, 2 * BM, BN);
+            uint32_t it = 0, acc_it = 0;
+            bool ok = true;
+            for (int u = pair; u < units && ok; u += npairs) {
+                for (int c = 0; c < nchunks && ok; ++c, ++acc_it) {
+                    const uint32_t buf = acc_it & 1;
+                    if (!tc::mbar_wait_cluster(&acce[buf], ((acc_it >> 1) & 1) ^ 1, p.err, kDevTimeoutAccEmpty)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t d_tmem = tmem + buf * BN;
+                    uint32_t accumulate = 0;
+                    const int kb1 = min(p.kb_count, (c + 1) * KB_PER_CHUNK);
+                    for (int kb = c * KB_PER_CHUNK; kb < kb1; ++kb, ++it) {
+                        const int st = it % STAGES;
+                        if (!tc::mbar_wait(&full[st], (it / STAGES) & 1, p.err, kDevTimeoutFull)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::tc_fence_after();
+                        const uint32_t sa = tc::smem_u32(smem + st * STAGE);
+                        const uint64_t ad = tc::sdesc_k_sw128(sa), bd = tc::sdesc_k_sw128(sa + A_STAGE);
+#pragma unroll
+                        for (int kk = 0; kk < BKE / 16; ++kk) {  // K = 16 per MMA: 32 bytes
+                            tc::mma_pair_f16(d_tmem, ad + 2 * kk, bd + 2 * kk, ID, accumulate);
+                            accumulate = 1;
+                        }
+                        tc::mma_pair_commit_multicast(&empty[st], 3);
+                    }
+                    if (ok) tc::mma_pair_commit_multicast(&accf[buf], 3);
+                }
+            }
+            tc::mma_pair_commit_multicast(drain, 1);  // every MMA complete before TMEM is released
+            tc::mbar_wait_drain(drain, 0);
+        }
+    } else {  // ------------------------------------------------ epilogue (both CTAs)
+        const int quad = warp & 3;             // TMEM lanes this warp may access
+        const int half = (warp - 2) >> 2;      // columns [half*128, half*128 + 128) of the tile
+        const int row = quad * 32 + lane;
+        const uint32_t acce0 = tc::mapa_shared(acce, 0);
+        uint32_t acc_it = 0;
+        bool ok = true;
+        for (int u = pair; u < units && ok; u += npairs) {
+            const int t = u / p.num_tiles, tile = u - t * p.num_tiles;
+            int mbp, nb;
+            oz::tile_coords(tile, num_pm, p.num_n_tiles, mbp, nb, kStripPairs);
+            const int mb = 2 * mbp + rank;
+            const uint32_t pm = p.p[t], mg = p.magic[t], bias = p.bias[t];
+            int s[4][32];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int j = 0; j < 32; ++j) s[q][j] = 0;
+            for (int c = 0; c < nchunks; ++c, ++acc_it) {
+                const uint32_t buf = acc_it & 1;
+                // all lanes must agree before the warp-collective TMEM loads
+                if (!__all_sync(0xffffffffu, tc::mbar_wait(&accf[buf], (acc_it >> 1) & 1, p.err, kDevTimeoutAcc))) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * BN + half * 128;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint32_t v[32];
+                    tc::tmem_ld_32x32b_x32(base + q * 32, v);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) s[q][j] += __float2int_rn(__uint_as_float(v[j]));
+                }
+                tc::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive_cluster(acce0 + buf * 8);
+                if ((c + 1) % CHUNKS_PER_REDUCE == 0) {  // keep |s| below 2^30 for any K
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) reduce_sums(s[q], pm, mg, bias);
+                }
+            }
+            if (!ok) break;
+            // residues of the 128 columns of this thread's row: 8 groups of 16
+            const int64_t i = (int64_t)mb * BM + row;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                reduce_sums(s[q], pm, mg, bias);
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    uint32_t w[4];
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) {
+                        const int j0 = g * 16 + b * 4;
+                        w[b] = (uint32_t)s[q][j0] | ((uint32_t)s[q][j0 + 1] << 8) | ((uint32_t)s[q][j0 + 2] << 16) |
+                               ((uint32_t)s[q][j0 + 3] << 24);
+                    }
+                    const int64_t jb = (int64_t)nb * (BN / 16) + half * 8 + q * 2 + g;
+                    *reinterpret_cast<uint4*>(p.R + (((int64_t)t * p.nb16 + jb) * p.m_pad + i) * 16) =
+                        make_uint4(w[0], w[1], w[2], w[3]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    tc::cluster_sync();  // the even CTA's MMAs read this CTA's shared memory and write its TMEM
+    if (warp == 1) {
+        __syncwarp();
+        tc::tc_fence_after();
+        tc::tmem_dealloc_pair(tmem, 512);
+    }
+}
+
+// ------------------------------------------------------------- reconstruction
+struct CombineParams {
+    int nmod, twoP;
+    int shift;        // bit offset of the quotient estimate (bit length of M minus 24)
+    float inv_mhi;    // 1 / (M >> shift)
+    uint32_t w[MAX_MODULI][LIMBS];  // CRT weights w_t = (M/p_t) * ((M/p_t)^-1 mod p_t)
+    uint32_t M[LIMBS], halfM[LIMBS];
+    int64_t m, n, ldc, m_pad, nb16, row_blocks;
+    int64_t n_split;  // complex: GEMM columns [0, n_split) are real parts, the rest imaginary parts
+    int cs;           // doubles per element of C (1 real, 2 complex)
+    const uint8_t* R;
+    const int* expA;
+    const int* expB;
+    double* C;
+    double alpha, beta;
+    int alpha_one, beta_zero;
+};
+
+// Bits [s, s + 64) of the L-limb integer x (static limb indices only).
+template <int L>
+__device__ __forceinline__ unsigned long long bits64(const uint32_t (&x)[L], int s) {
+    unsigned long long v = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        const int pos = 32 * l - s;  // where bit 0 of limb l lands
+        if (pos >= 64 || pos <= -32) continue;
+        const unsigned long long limb = x[l];
+        v |= pos >= 0 ? (limb << pos) : (limb >> -pos);
+    }
+    return v;
+}
+
+// Whether any bit below bit s of x is set.
+template <int L>
+__device__ __forceinline__ bool any_below(const uint32_t (&x)[L], int s) {
+    uint32_t any = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        const int lo = 32 * l;
+        if (lo + 32 <= s) any |= x[l];
+        else if (lo < s) any |= x[l] & ((1u << (s - lo)) - 1u);
+    }
+    return any != 0;
+}
+
+// x -= y (returns the borrow out).
+template <int L>
+__device__ __forceinline__ uint32_t sub_limbs(uint32_t (&x)[L], const uint32_t* y) {
+    unsigned long long br = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        const unsigned long long d = (unsigned long long)x[l] - y[l] - br;
+        x[l] = (uint32_t)d;
+        br = (d >> 63) & 1ull;
+    }
+    return (uint32_t)br;
+}
+template <int L>
+__device__ __forceinline__ void add_limbs(uint32_t (&x)[L], const uint32_t* y) {
+    unsigned long long c = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        c += (unsigned long long)x[l] + y[l];
+        x[l] = (uint32_t)c;
+        c >>= 32;
+    }
+}
+// Sign of x - y: the highest differing limb decides.
+template <int L>
+__device__ __forceinline__ int cmp_limbs(const uint32_t (&x)[L], const uint32_t* y) {
+    int c = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+        if (x[l] != y[l]) c = x[l] > y[l] ? 1 : -1;
+    return c;
+}
+
+// One output element per thread: a block of 16 warps covers 32 rows x 16
+// GEMM columns (block b: row block b % row_blocks, column block b /
+// row_blocks); warp w takes column 16*cb + w, lane the row 32*rb + lane, so
+// that the 16 warps read the 512 contiguous residue bytes of each modulus
+// together.
+template <int L>
+__global__ void __launch_bounds__(512) combine_kernel(const __grid_constant__ CombineParams p) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t rb = (int64_t)blockIdx.x % p.row_blocks, cb = (int64_t)blockIdx.x / p.row_blocks;
+    const int64_t i = rb * 32 + lane;
+    const int64_t gj = cb * 16 + w;  // GEMM column
+    int64_t j = gj;
+    int part = 0;
+    if (j >= p.n_split) {
+        j -= p.n_split;
+        part = 1;
+    }
+    if (i >= p.m || j >= p.n) return;
+    const uint8_t* rp = p.R + (cb * p.m_pad + i) * 16 + w;
+    const int64_t stride = p.nb16 * p.m_pad * 16;
+    unsigned long long acc[L];
+#pragma unroll
+    for (int l = 0; l < L; ++l) acc[l] = 0;
+#pragma unroll 4
+    for (int t = 0; t < p.nmod; ++t) {
+        const uint32_t r = rp[t * stride];
+#pragma unroll
+        for (int l = 0; l < L; ++l) acc[l] += (unsigned long long)r * p.w[t][l];
+    }
+    uint32_t x[L];
+    unsigned long long c = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        c += acc[l];
+        x[l] = (uint32_t)c;
+        c >>= 32;
+    }
+    // x mod M: the quotient estimate is floor(x/M) or off by one either way
+    const unsigned long long xh = bits64<L>(x, p.shift);
+    const uint32_t q = (uint32_t)((float)xh * p.inv_mhi);
+    if (q) {
+        unsigned long long br = 0, cm = 0;
+#pragma unroll
+        for (int l = 0; l < L; ++l) {  // x -= q * M
+            cm += (unsigned long long)q * p.M[l];
+            const unsigned long long d = (unsigned long long)x[l] - (uint32_t)cm - br;
+            x[l] = (uint32_t)d;
+            br = (d >> 63) & 1ull;
+            cm >>= 32;
+        }
+        if (br) add_limbs<L>(x, p.M);  // the estimate was one too large
+    }
+    if (cmp_limbs<L>(x, p.M) >= 0) sub_limbs<L>(x, p.M);
+    // centre: values above M/2 stand for x - M
+    const bool neg = cmp_limbs<L>(x, p.halfM) > 0;
+    if (neg) {
+        uint32_t y[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) y[l] = p.M[l];
+        sub_limbs<L>(y, x);
+#pragma unroll
+        for (int l = 0; l < L; ++l) x[l] = y[l];
+    }
+    // round |V| * 2^(E_i + F_j - 2P) once to FP64: the top 127 bits with the
+    // bits below folded into a sticky last bit (below the rounding position
+    // whenever bits were dropped, so round-to-nearest-even is unaffected)
+    int top = -1;
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+        if (x[l]) top = 32 * l + 31 - __clz((int)x[l]);
+    double r = 0.0;
+    if (top >= 0) {
+        const int e2 = p.expA[i] + p.expB[j] - p.twoP;
+        const int b0 = top > 126 ? top - 126 : 0;  // bit 127 of the window stays clear: it is the sign
+        unsigned long long lo = bits64<L>(x, b0), hi = bits64<L>(x, b0 + 64);
+        if (b0 > 0 && any_below<L>(x, b0)) lo |= 1ull;
+        r = oz::i128_to_double(lo, hi, e2 + b0);
+        if (neg) r = -r;
+    }
+    double* cp = p.C + (i + j * p.ldc) * p.cs + part;
+    if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
+    if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+    *cp = r;
+}
+
+// ---------------------------------------------------------------- host side
+struct Big {  // little-endian 32-bit limbs
+    uint32_t w[LIMBS] = {};
+    void mul_small(uint32_t x) {
+        unsigned long long c = 0;
+        for (int i = 0; i < LIMBS; ++i) {
+            c += (unsigned long long)w[i] * x;
+            w[i] = (uint32_t)c;
+            c >>= 32;
+        }
+    }
+    uint32_t mod_small(uint32_t p) const {
+        unsigned long long r = 0;
+        for (int i = LIMBS - 1; i >= 0; --i) r = ((r << 32) | w[i]) % p;
+        return (uint32_t)r;
+    }
+    int bitlen() const {
+        for (int i = LIMBS - 1; i >= 0; --i)
+            if (w[i]) return 32 * i + 32 - __builtin_clz(w[i]);
+        return 0;
+    }
+    unsigned long long bits64(int s) const {
+        unsigned long long v = 0;
+        for (int l = 0; l < LIMBS; ++l) {
+            const int pos = 32 * l - s;
+            if (pos >= 64 || pos <= -32) continue;
+            const unsigned long long limb = w[l];
+            v |= pos >= 0 ? (limb << pos) : (limb >> -pos);
+        }
+        return v;
+    }
+};
+
+uint32_t inverse_mod(uint32_t a, uint32_t p) {  // a^-1 mod p, gcd(a, p) = 1
+    long long t = 0, nt = 1, r = p, nr = a % p;
+    while (nr) {
+        const long long q = r / nr;
+        std::swap(t, nt);
+        nt -= q * t;
+        std::swap(r, nr);
+        nr -= q * r;
+    }
+    return (uint32_t)(t < 0 ? t + p : t);
+}
+
+Big modulus_product(int nmod) {
+    Big M;
+    M.w[0] = 1;
+    for (int t = 0; t < nmod; ++t) M.mul_small(kModuli[t]);
+    return M;
+}
+
+int ceil_log2(int64_t k) {
+    int b = 0;
+    while (((int64_t)1 << b) < k) ++b;
+    return b;
+}
+
+// Largest P with M >= 2^(2P + ceil(log2 k) + 2), i.e. M > 4 k 2^(2P) > 2 max|V|.
+int max_fraction_bits(int nmod, int64_t k) { return (modulus_product(nmod).bitlen() - 1 - ceil_log2(k) - 2) / 2; }
+
+// Fraction bits the requested accuracy needs for inputs with this exponent
+// spread: the calibrated width of the slice form (oz::required_fraction_bits)
+// plus COSMA_GPU_OZAKI2_EXTRA_BITS.
+int requested_fraction_bits(double spread, int64_t k) {
+    static const long long extra = env_ll("COSMA_GPU_OZAKI2_EXTRA_BITS", 0);
+    return (int)std::ceil(oz::required_fraction_bits(spread, k)) + (int)extra;
+}
+
+// Modulus count and fraction bits: the caller's count, or the fewest moduli
+// whose product admits the requested fraction bits; P is then the largest
+// the count allows.
+int choose(int nmod_req, double spread, int64_t k, int* nmod, int* P) {
+    if (nmod_req > 0) {
+        *nmod = std::min(nmod_req, MAX_MODULI);
+    } else {
+        const int want = requested_fraction_bits(spread, k);
+        *nmod = MAX_MODULI;
+        for (int t = 2; t <= MAX_MODULI; ++t)
+            if (max_fraction_bits(t, k) >= want) {
+                *nmod = t;
+                break;
+            }
+    }
+    *P = std::min(max_fraction_bits(*nmod, k), 120);  // shifts of the split stay below 128
+    if (*P < 1) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2: too few moduli for this k");
+    return COSMA_GPU_SUCCESS;
+}
+
+void fill_split(SplitParams& sp, int nmod, int P) {
+    std::memset(&sp, 0, sizeof(sp));
+    sp.nmod = nmod;
+    sp.P = P;
+    for (int t = 0; t < nmod; ++t) {
+        const uint32_t p = kModuli[t];
+        sp.p[t] = p;
+        sp.magic[t] = (uint32_t)((1ull << 32) / p);
+        sp.c32[t] = (uint32_t)((1ull << 32) % p);
+    }
+}
+
+void fill_combine(CombineParams& cp, int nmod, int P) {
+    std::memset(&cp, 0, sizeof(cp));
+    cp.nmod = nmod;
+    cp.twoP = 2 * P;
+    const Big M = modulus_product(nmod);
+    for (int t = 0; t < nmod; ++t) {
+        Big Mt;
+        Mt.w[0] = 1;
+        for (int s = 0; s < nmod; ++s)
+            if (s != t) Mt.mul_small(kModuli[s]);
+        const uint32_t y = inverse_mod(Mt.mod_small(kModuli[t]), kModuli[t]);
+        Mt.mul_small(y);
+        std::memcpy(cp.w[t], Mt.w, sizeof(Mt.w));
+    }
+    std::memcpy(cp.M, M.w, sizeof(M.w));
+    for (int l = 0; l < LIMBS; ++l) cp.halfM[l] = (M.w[l] >> 1) | (l + 1 < LIMBS ? (M.w[l + 1] << 31) : 0u);
+    cp.shift = std::max(0, M.bitlen() - 24);
+    cp.inv_mhi = 1.0f / (float)M.bits64(cp.shift);
+}
+
+// Limbs the reconstruction needs: sum_t r_t w_t < nmod * 255 * M.
+int limbs_for(int nmod) { return (modulus_product(nmod).bitlen() + 13 + 31) / 32; }
+
+struct Workspace {
+    DeviceBuffer resA, resB, expA, expB, part, R, stats, err;
+    DeviceBuffer T;  // complex alpha/beta: the product before alpha*T + beta*C
+    Stats* host_stats = nullptr;
+    unsigned* host_err = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+std::mutex g_ws_mu;
+std::map<std::pair<int, cudaStream_t>, Workspace*> g_ws;
+
+Workspace* workspace(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_ws_mu);
+    auto& w = g_ws[{dev, s}];
+    if (!w) {
+        w = new Workspace();
+        if (cudaMallocHost(&w->host_stats, sizeof(Stats)) != cudaSuccess) w->host_stats = nullptr;
+        if (cudaMallocHost(&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
+        for (auto& e : w->ev)
+            if (cudaEventCreate(&e) != cudaSuccess) e = nullptr;
+        cudaGetLastError();
+    }
+    return w;
+}
+
+int pair_grid(int units, int* grid) {
+    static PerDevice<int> pairs;
+    int n = 0;
+    CGB_CHECK(pairs.get(
+        [](int& v) {
+            CGB_CUDA(cudaFuncSetAttribute(gemm_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(2 * device_sm_count(), 1, 1);
+            cfg.blockDim = dim3(THREADS, 1, 1);
+            cfg.dynamicSmemBytes = SMEM_BYTES;
+            cudaLaunchAttribute attr;
+            attr.id = cudaLaunchAttributeClusterDimension;
+            attr.val.clusterDim.x = 2;
+            attr.val.clusterDim.y = 1;
+            attr.val.clusterDim.z = 1;
+            cfg.attrs = &attr;
+            cfg.numAttrs = 1;
+            CGB_CUDA(cudaOccupancyMaxActiveClusters(&v, gemm_pair_kernel, &cfg));
+            v = std::min(v, device_sm_count() / 2);
+            if (v < 1) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: no CTA pair of the GEMM fits on the GPU");
+            return COSMA_GPU_SUCCESS;
+        },
+        &n));
+    *grid = 2 * std::min(units, n);
+    return COSMA_GPU_SUCCESS;
+}
+
+int launch_gemm(const void* resA, const void* resB, int64_t k_pad, const GemmParams& p, cudaStream_t st) {
+    CUtensorMap tmA, tmB;
+    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, resA, (uint64_t)k_pad,
+                           (uint64_t)p.nmod * p.a_rows_pad, (uint64_t)k_pad * 2, BKE, BM));
+    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, resB, (uint64_t)k_pad,
+                           (uint64_t)p.nmod * p.b_rows_pad, (uint64_t)k_pad * 2, BKE, BN / 2));
+    int grid = 0;
+    CGB_CHECK(pair_grid(p.nmod * p.num_tiles, &grid));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid, 1, 1);
+    cfg.blockDim = dim3(THREADS, 1, 1);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.stream = st;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = 2;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    CGB_CUDA(cudaLaunchKernelEx(&cfg, gemm_pair_kernel, tmA, tmB, p));
+    return COSMA_GPU_SUCCESS;
+}
+
+int launch_combine(CombineParams& cp, int nmod, int64_t gemm_cols, cudaStream_t st) {
+    cp.row_blocks = ceil_div(cp.m, 32);
+    const int64_t blocks = cp.row_blocks * ceil_div(gemm_cols, 16);
+    if (blocks > 0x7FFFFFFF) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: C too large for the combine grid");
+    const unsigned grid = (unsigned)blocks;
+    switch (limbs_for(nmod)) {
+        case 1: case 2: case 3: case 4: combine_kernel<4><<<grid, 512, 0, st>>>(cp); break;
+        case 5: combine_kernel<5><<<grid, 512, 0, st>>>(cp); break;
+        case 6: combine_kernel<6><<<grid, 512, 0, st>>>(cp); break;
+        case 7: combine_kernel<7><<<grid, 512, 0, st>>>(cp); break;
+        default: combine_kernel<8><<<grid, 512, 0, st>>>(cp); break;
+    }
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
+}
+
+void fill_gemm(GemmParams& p, int nmod, int64_t m_pad, int64_t n_pad, int64_t k_pad, void* R, unsigned* err) {
+    std::memset(&p, 0, sizeof(p));
+    p.num_m_tiles = (int)(m_pad / BM);
+    p.num_n_tiles = (int)(n_pad / BN);
+    p.num_tiles = (p.num_m_tiles / 2) * p.num_n_tiles;
+    p.nmod = nmod;
+    p.kb_count = (int)(k_pad / BKE);
+    p.a_rows_pad = (int)m_pad;
+    p.b_rows_pad = (int)n_pad;
+    p.m_pad = m_pad;
+    p.nb16 = n_pad / 16;
+    p.R = (uint8_t*)R;
+    for (int t = 0; t < nmod; ++t) {
+        const uint32_t q = kModuli[t];
+        p.p[t] = q;
+        p.magic[t] = (uint32_t)((1ull << 32) / q);
+        p.bias[t] = (uint32_t)((((1ull << 30) + q - 1) / q) * q);
+    }
+    p.err = err;
+}
+
+// Shared front end: row scaling, statistics read-back, choice of N and P.
+// Returns with *fallback set when the inputs hold Inf/NaN.
+struct Plan {
+    int nmod = 0, P = 0;
+    double spread = 0.0;
+    bool fallback = false;
+};
+
+int finish_info(cosma_gpu_ozaki_info* info, Workspace* w, const Plan& pl, int64_t kb_count) {
+    if (!info) return COSMA_GPU_SUCCESS;
+    float prep = 0.f, gemm = 0.f;
+    cudaEventElapsedTime(&prep, w->ev[0], w->ev[1]);
+    cudaEventElapsedTime(&gemm, w->ev[2], w->ev[3]);
+    info->slices = pl.nmod;
+    info->products = pl.nmod;
+    info->fraction_bits = pl.P;
+    info->groups = pl.nmod * (int)((kb_count + KB_PER_CHUNK - 1) / KB_PER_CHUNK);
+    info->spread_bits = pl.spread;
+    info->prep_ms += prep;
+    info->gemm_ms += gemm;
+    return COSMA_GPU_SUCCESS;
+}
+
+int check_device_error(Workspace* w, cudaStream_t st) {
+    CGB_CUDA(cudaMemcpyAsync(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    if (*w->host_err)
+        return set_error(COSMA_GPU_ERROR_DEVICE_TIMEOUT,
+                         "ozaki2 gemm: a pipeline wait timed out (device code " + std::to_string(*w->host_err) + ")");
+    return COSMA_GPU_SUCCESS;
+}
+
+int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info* info) {
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
+    const double* A = (const double*)g.A;
+    const double* B = (const double*)g.B;
+    Workspace* w = workspace(st);
+    if (!w->host_stats || !w->host_err) return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "ozaki2: pinned staging");
+    if (!w->ev[0] || !w->ev[3]) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: timing events");
+    const int64_t m_pad = ceil_div(m, 2 * BM) * 2 * BM, n_pad = ceil_div(n, BN) * BN, k_pad = ceil_div(k, BKE) * BKE;
+
+    // 1. scaling + spread statistics
+    CGB_CHECK(w->stats.reserve(sizeof(Stats), st));
+    CGB_CHECK(w->err.reserve(sizeof(unsigned), st));
+    CGB_CHECK(w->expA.reserve((size_t)m_pad * 4, st));
+    CGB_CHECK(w->expB.reserve((size_t)n_pad * 4, st));
+    Stats* st_dev = (Stats*)w->stats.ptr;
+    CGB_CUDA(cudaEventRecord(w->ev[0], st));
+    CGB_CUDA(cudaMemsetAsync(st_dev, 0, sizeof(Stats), st));
+    CGB_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(unsigned), st));
+    CGB_CUDA(cudaMemsetAsync(w->expA.ptr, 0, (size_t)m_pad * 4, st));
+    CGB_CUDA(cudaMemsetAsync(w->expB.ptr, 0, (size_t)n_pad * 4, st));
+    CGB_CHECK(oz::scale_operand(a_kc, A, g.lda, m, k, (int*)w->expA.ptr, w->part, st_dev, 0, st, 1));
+    CGB_CHECK(oz::scale_operand(b_kc, B, g.ldb, n, k, (int*)w->expB.ptr, w->part, st_dev, 1, st, 1));
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, st_dev, sizeof(Stats), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    const Stats hs = *w->host_stats;
+    Plan pl;
+    pl.spread = (double)hs.spread[0] + (double)hs.spread[1];
+    if (hs.nonfinite) {  // Inf/NaN have no residues: the native FP64 kernel propagates them
+        if (info) info->fallback_native = 1;
+        return native_gemm(g, st);
+    }
+    CGB_CHECK(choose(nmod_req, pl.spread, k, &pl.nmod, &pl.P));
+
+    // 2. residue matrices
+    const size_t resA_bytes = (size_t)pl.nmod * m_pad * k_pad * 2, resB_bytes = (size_t)pl.nmod * n_pad * k_pad * 2;
+    CGB_CHECK(w->resA.reserve(resA_bytes, st));
+    CGB_CHECK(w->resB.reserve(resB_bytes, st));
+    SplitParams sp;
+    fill_split(sp, pl.nmod, pl.P);
+    {
+        dim3 gA((unsigned)(m_pad / 32), (unsigned)(k_pad / 64)), gB((unsigned)(n_pad / 32), (unsigned)(k_pad / 64));
+        if (gA.y > 65535 || gB.y > 65535) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: k too large");
+        uint16_t* rA = (uint16_t*)w->resA.ptr;
+        uint16_t* rB = (uint16_t*)w->resB.ptr;
+        if (a_kc) split_kernel<true><<<gA, 256, 0, st>>>(A, g.lda, m, k, (const int*)w->expA.ptr, k_pad, m_pad, rA, sp);
+        else split_kernel<false><<<gA, 256, 0, st>>>(A, g.lda, m, k, (const int*)w->expA.ptr, k_pad, m_pad, rA, sp);
+        if (b_kc) split_kernel<true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, (const int*)w->expB.ptr, k_pad, n_pad, rB, sp);
+        else split_kernel<false><<<gB, 256, 0, st>>>(B, g.ldb, n, k, (const int*)w->expB.ptr, k_pad, n_pad, rB, sp);
+        CGB_CUDA(cudaGetLastError());
+    }
+    CGB_CUDA(cudaEventRecord(w->ev[1], st));
+
+    // 3. modular GEMMs -> residue bytes
+    CGB_CHECK(w->R.reserve((size_t)pl.nmod * m_pad * n_pad, st));
+    GemmParams gp;
+    fill_gemm(gp, pl.nmod, m_pad, n_pad, k_pad, w->R.ptr, (unsigned*)w->err.ptr);
+    CGB_CUDA(cudaEventRecord(w->ev[2], st));
+    CGB_CHECK(launch_gemm(w->resA.ptr, w->resB.ptr, k_pad, gp, st));
+    CGB_CUDA(cudaEventRecord(w->ev[3], st));
+
+    // 4. reconstruction, scaling, alpha and beta
+    CombineParams cp;
+    fill_combine(cp, pl.nmod, pl.P);
+    cp.m = m;
+    cp.n = n;
+    cp.ldc = g.ldc;
+    cp.m_pad = m_pad;
+    cp.nb16 = n_pad / 16;
+    cp.n_split = INT64_MAX;
+    cp.cs = 1;
+    cp.R = (const uint8_t*)w->R.ptr;
+    cp.expA = (const int*)w->expA.ptr;
+    cp.expB = (const int*)w->expB.ptr;
+    cp.C = (double*)g.C;
+    cp.alpha = g.alpha[0];
+    cp.beta = g.beta[0];
+    cp.alpha_one = g.alpha[0] == 1.0;
+    cp.beta_zero = g.beta[0] == 0.0;
+    CGB_CHECK(launch_combine(cp, pl.nmod, n, st));
+    CGB_CHECK(check_device_error(w, st));
+    return finish_info(info, w, pl, gp.kb_count);
+}
+
+int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info* info) {
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const bool a_kc = g.opa != 0, b_kc = g.opb == 0;
+    const double2* A = (const double2*)g.A;
+    const double2* B = (const double2*)g.B;
+    Workspace* w = workspace(st);
+    if (!w->host_stats || !w->host_err) return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "ozaki2: pinned staging");
+    if (!w->ev[0] || !w->ev[3]) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: timing events");
+    const int64_t m_pad = ceil_div(m, 2 * BM) * 2 * BM, nh = ceil_div(n, BN) * BN, kh = ceil_div(k, BKE) * BKE;
+    const int64_t k_pad = 2 * kh, n_pad = 2 * nh;
+
+    CGB_CHECK(w->stats.reserve(sizeof(Stats), st));
+    CGB_CHECK(w->err.reserve(sizeof(unsigned), st));
+    CGB_CHECK(w->expA.reserve((size_t)m_pad * 4, st));
+    CGB_CHECK(w->expB.reserve((size_t)nh * 4, st));
+    Stats* st_dev = (Stats*)w->stats.ptr;
+    CGB_CUDA(cudaEventRecord(w->ev[0], st));
+    CGB_CUDA(cudaMemsetAsync(st_dev, 0, sizeof(Stats), st));
+    CGB_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(unsigned), st));
+    CGB_CUDA(cudaMemsetAsync(w->expA.ptr, 0, (size_t)m_pad * 4, st));
+    CGB_CUDA(cudaMemsetAsync(w->expB.ptr, 0, (size_t)nh * 4, st));
+    CGB_CHECK(oz::scale_operand(a_kc, (const double*)A, g.lda, m, k, (int*)w->expA.ptr, w->part, st_dev, 0, st, 2));
+    CGB_CHECK(oz::scale_operand(b_kc, (const double*)B, g.ldb, n, k, (int*)w->expB.ptr, w->part, st_dev, 1, st, 2));
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, st_dev, sizeof(Stats), cudaMemcpyDeviceToHost, st));
+    CGB_CUDA(cudaStreamSynchronize(st));
+    const Stats hs = *w->host_stats;
+    Plan pl;
+    pl.spread = (double)hs.spread[0] + (double)hs.spread[1];
+    if (hs.nonfinite) {
+        if (info) info->fallback_native = 1;
+        return native_gemm(g, st);
+    }
+    CGB_CHECK(choose(nmod_req, pl.spread, 2 * k, &pl.nmod, &pl.P));
+
+    CGB_CHECK(w->resA.reserve((size_t)pl.nmod * m_pad * k_pad * 2, st));
+    CGB_CHECK(w->resB.reserve((size_t)pl.nmod * n_pad * k_pad * 2, st));
+    SplitParams sp;
+    fill_split(sp, pl.nmod, pl.P);
+    {
+        dim3 gA((unsigned)(m_pad / 32), (unsigned)(kh / 64)), gB((unsigned)(nh / 32), (unsigned)(kh / 64));
+        if (gA.y > 65535) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: k too large");
+        uint16_t* rA = (uint16_t*)w->resA.ptr;
+        uint16_t* rB = (uint16_t*)w->resB.ptr;
+        const int ca = g.opa == 2, cb = g.opb == 2;
+        const int* eA = (const int*)w->expA.ptr;
+        const int* eB = (const int*)w->expB.ptr;
+        if (a_kc) split_cplx_kernel<true, false><<<gA, 256, 0, st>>>(A, g.lda, m, k, eA, kh, m_pad, m_pad, ca, rA, sp);
+        else split_cplx_kernel<false, false><<<gA, 256, 0, st>>>(A, g.lda, m, k, eA, kh, m_pad, m_pad, ca, rA, sp);
+        if (b_kc) split_cplx_kernel<true, true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, eB, kh, nh, n_pad, cb, rB, sp);
+        else split_cplx_kernel<false, true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, eB, kh, nh, n_pad, cb, rB, sp);
+        CGB_CUDA(cudaGetLastError());
+    }
+    CGB_CUDA(cudaEventRecord(w->ev[1], st));
+
+    CGB_CHECK(w->R.reserve((size_t)pl.nmod * m_pad * n_pad, st));
+    GemmParams gp;
+    fill_gemm(gp, pl.nmod, m_pad, n_pad, k_pad, w->R.ptr, (unsigned*)w->err.ptr);
+    CGB_CUDA(cudaEventRecord(w->ev[2], st));
+    CGB_CHECK(launch_gemm(w->resA.ptr, w->resB.ptr, k_pad, gp, st));
+    CGB_CUDA(cudaEventRecord(w->ev[3], st));
+
+    // real alpha and beta are applied by the combine kernel, complex ones by
+    // alpha*T + beta*C afterwards
+    const bool fused = g.alpha[1] == 0.0 && g.beta[1] == 0.0;
+    CombineParams cp;
+    fill_combine(cp, pl.nmod, pl.P);
+    cp.m = m;
+    cp.n = n;
+    cp.m_pad = m_pad;
+    cp.nb16 = n_pad / 16;
+    cp.n_split = nh;
+    cp.cs = 2;
+    cp.R = (const uint8_t*)w->R.ptr;
+    cp.expA = (const int*)w->expA.ptr;
+    cp.expB = (const int*)w->expB.ptr;
+    if (fused) {
+        cp.C = (double*)g.C;
+        cp.ldc = g.ldc;
+        cp.alpha = g.alpha[0];
+        cp.beta = g.beta[0];
+    } else {
+        CGB_CHECK(w->T.reserve((size_t)m * n * 16, st));
+        cp.C = (double*)w->T.ptr;
+        cp.ldc = m;
+        cp.alpha = 1.0;
+        cp.beta = 0.0;
+    }
+    cp.alpha_one = cp.alpha == 1.0;
+    cp.beta_zero = cp.beta == 0.0;
+    CGB_CHECK(launch_combine(cp, pl.nmod, n_pad, st));
+    CGB_CHECK(check_device_error(w, st));
+    if (!fused) CGB_CHECK(unpack_device(Scalar::Z, m, n, g.alpha, w->T.ptr, m, g.beta, g.C, g.ldc, st));
+    return finish_info(info, w, pl, gp.kb_count);
+}
+
+}  // namespace oz2
+
+}  // namespace cgb
+
+extern "C" int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int moduli, int* nmod, int* fraction_bits) {
+    cgb::clear_error();
+    if (k < 1 || !nmod || !fraction_bits)
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2_choose: k >= 1 and output pointers needed");
+    return cgb::oz2::choose(moduli, spread_bits, k, nmod, fraction_bits);
+}
+
+namespace cgb {
+
+int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
+    if (g.scalar != Scalar::D) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: double only");
+    if (((uintptr_t)g.A | (uintptr_t)g.B | (uintptr_t)g.C) % 8)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: buffers must be 8-byte aligned");
+    if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: m and n are limited to 2^24");
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    // one pass is exact for k up to KMAX (the split grid's K extent); longer
+    // K runs in passes accumulated through C (beta = 1 after the first)
+    GemmDesc c = g;
+    for (int64_t k0 = 0; k0 < g.k; k0 += oz2::KMAX) {
+        c.k = std::min<int64_t>(oz2::KMAX, g.k - k0);
+        c.A = (const double*)g.A + (g.opa == 0 ? k0 * g.lda : k0);
+        c.B = (const double*)g.B + (g.opb == 0 ? k0 : k0 * g.ldb);
+        if (k0 > 0) { c.beta[0] = 1.0; c.beta[1] = 0.0; }
+        CGB_CHECK(oz2::dgemm(c, moduli, stream, info));
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+int ozaki2_zgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
+    if (g.scalar != Scalar::Z) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: complex double only");
+    if (((uintptr_t)g.A | (uintptr_t)g.B | (uintptr_t)g.C) % 16)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: complex buffers must be 16-byte aligned");
+    if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 23)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: m is limited to 2^24 and n to 2^23 (complex)");
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    const int64_t kmax = oz2::KMAX / 2;  // each complex term is two real terms
+    GemmDesc c = g;
+    for (int64_t k0 = 0; k0 < g.k; k0 += kmax) {
+        c.k = std::min<int64_t>(kmax, g.k - k0);
+        c.A = (const double2*)g.A + (g.opa == 0 ? k0 * g.lda : k0);
+        c.B = (const double2*)g.B + (g.opb == 0 ? k0 : k0 * g.ldb);
+        if (k0 > 0) { c.beta[0] = 1.0; c.beta[1] = 0.0; }
+        CGB_CHECK(oz2::zgemm(c, moduli, stream, info));
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace cgb

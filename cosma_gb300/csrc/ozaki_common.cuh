@@ -6,6 +6,7 @@
 
 #include "common.cuh"
 #include "tc_common.cuh"
+#include "runtime.hpp"
 
 #include <cuda_fp8.h>
 
@@ -366,7 +367,16 @@ __device__ __forceinline__ bool epilogue_tile(const P& p, const Schedule& sc, in
 }
 
 // Host helpers defined in ozaki.cu.
+// Row exponents (1 + floor(log2 max |x|)) and spread statistics of a
+// (rows x k) operand; kcontig: element (r, l) at X[l + r*ld], else at
+// X[r + l*ld]; es = 2 for complex operands (ld in complex elements).  `part`
+// holds the partial states of the row-contiguous form.
+int scale_operand(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, int* exps, DeviceBuffer& part,
+                  Stats* st_dev, int which, cudaStream_t st, int es);
 int num_sms();
+// Fraction bits of the operands' fixed-point form that reach ~1e-15 relative
+// accuracy for this exponent spread and depth (calibrated on u*2^e inputs).
+double required_fraction_bits(double spread_bits, int64_t k);
 int choose_slices(double spread_bits, int64_t k);
 int build_schedule(int S, int64_t k, int64_t k_pad, int a_rows_pad, int b_rows_pad, Schedule* sc, int* L);
 

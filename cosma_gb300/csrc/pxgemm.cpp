@@ -244,7 +244,7 @@ CGB_PX_FAMILY(COSMA_PSGEMM, COSMA_PDGEMM, COSMA_PCGEMM, COSMA_PZGEMM)
 CGB_PX_FAMILY(COSMA_PSGEMM_, COSMA_PDGEMM_, COSMA_PCGEMM_, COSMA_PZGEMM_)
 
 int cosma_gpu_pxgemm_set_method(int method) {
-    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_BF16X3)
+    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_OZAKI2)
         return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "pxgemm_set_method: unknown method");
     std::lock_guard<std::mutex> lock(cgb::g_px_mu);
     cgb::g_px_method = method;

@@ -90,6 +90,7 @@ int default_method() {
     std::transform(s.begin(), s.end(), s.begin(), [](unsigned char c) { return (char)std::tolower(c); });
     if (s == "native") return COSMA_GPU_METHOD_NATIVE;
     if (s == "ozaki") return COSMA_GPU_METHOD_OZAKI;
+    if (s == "ozaki2") return COSMA_GPU_METHOD_OZAKI2;
     if (s == "bf16x3") return COSMA_GPU_METHOD_BF16X3;
     return COSMA_GPU_METHOD_AUTO;
 }

@@ -121,6 +121,10 @@ int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, co
 int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t cols, const void* src, int64_t lds,
                 void* dst, int64_t ldd, cudaStream_t s);
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t stream);         // bf16x3.cu
+int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream,
+                 cosma_gpu_ozaki_info* info);                    // ozaki2.cu
+int ozaki2_zgemm(const GemmDesc& g, int moduli, cudaStream_t stream,
+                 cosma_gpu_ozaki_info* info);                    // ozaki2.cu
 
 // The method of the process-wide entry points (p?gemm, multiply_using_layout):
 // cosma_gpu_pxgemm_set_method, else COSMA_GPU_GEMM_METHOD (pxgemm.cpp).

@@ -232,6 +232,15 @@ __device__ __forceinline__ void mma_pair_f8f6f4(uint32_t d_tmem, uint64_t adesc,
         "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}"
         ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
+// The same for the 16-bit kinds (BF16 / F16 inputs) over the pair.
+__device__ __forceinline__ void mma_pair_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                             uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
 // Arrives on the mbarrier at the same offset in every CTA of `mask` once the
 // pair MMAs issued so far have completed.
 __device__ __forceinline__ void mma_pair_commit_multicast(uint64_t* bar, uint16_t mask) {

@@ -166,7 +166,7 @@ int tmm_gemm(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int64_t m, int
     const bool dA = is_device_ptr(A), dB = is_device_ptr(B), dC = is_device_ptr(C);
     const bool trivial = (k == 0) || is_zero(alpha, sc);
     cosma_gpu_ozaki_info* info = &h->last_info;
-    *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
+    *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
 
     if (trivial && is_one(beta, sc)) return COSMA_GPU_SUCCESS;  // C unchanged
     if (dC && (trivial || (dA && dB))) {  // everything already in HBM
@@ -427,7 +427,7 @@ void cosma_gpu_tmm_destroy_context(cosma_gpu_mm_handle* h) {
 int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* h, int method, int slices) {
     cgb::clear_error();
     if (!h) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "set_method: null handle");
-    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_BF16X3)
+    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_OZAKI2)
         return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "set_method: unknown method");
     std::lock_guard<std::mutex> lock(h->mu);
     h->method = method;
@@ -443,7 +443,11 @@ static double tmm_footprint(cgb::Scalar s, int method, double t) {
     const double es = (double)cgb::scalar_bytes(s);
     double bytes = 2.0 * 3.0 * t * t * es;
     if (method == COSMA_GPU_METHOD_AUTO) method = s == cgb::Scalar::S ? COSMA_GPU_METHOD_BF16X3 : COSMA_GPU_METHOD_NATIVE;
-    if (method == COSMA_GPU_METHOD_OZAKI && s == cgb::Scalar::S) method = COSMA_GPU_METHOD_BF16X3;
+    if ((method == COSMA_GPU_METHOD_OZAKI || method == COSMA_GPU_METHOD_OZAKI2) && s == cgb::Scalar::S)
+        method = COSMA_GPU_METHOD_BF16X3;
+    // residue matrices (BF16) of both operands and residue bytes of C, at the largest modulus count
+    if (method == COSMA_GPU_METHOD_OZAKI2 && s == cgb::Scalar::D) bytes += 28.0 * (2.0 * 2.0 + 1.0) * t * t;
+    if (method == COSMA_GPU_METHOD_OZAKI2 && s == cgb::Scalar::Z) bytes += 28.0 * 14.0 * t * t + 16.0 * t * t;
     if (method == COSMA_GPU_METHOD_OZAKI && s == cgb::Scalar::D)
         bytes += 16.0 * 2.0 * t * t + 152.0 * 128 * 256 * 16;
     if (method == COSMA_GPU_METHOD_OZAKI && s == cgb::Scalar::Z)
@@ -461,7 +465,7 @@ int cosma_gpu_tmm_tiles_for_memory(char scalar, int method, int64_t bytes, int* 
     cgb::Scalar s;
     if (!parse_scalar(scalar, &s) || !tile_m || !tile_n || !tile_k)
         return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "tiles_for_memory: bad argument");
-    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_BF16X3)
+    if (method < COSMA_GPU_METHOD_AUTO || method > COSMA_GPU_METHOD_OZAKI2)
         return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "tiles_for_memory: unknown method");
     int64_t best = 0;
     for (int64_t t = 256; t <= (1 << 20); t += 256) {

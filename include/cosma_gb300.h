@@ -61,6 +61,11 @@ int cosma_gpu_selftest_wait_timeout(unsigned long long limit_ns, void* stream);
 #define COSMA_GPU_METHOD_NATIVE 1
 #define COSMA_GPU_METHOD_OZAKI 2
 #define COSMA_GPU_METHOD_BF16X3 3
+/* FP64-accurate GEMM by the Chinese-remainder form of the Ozaki scheme
+ * (Ozaki scheme II): one BF16 tensor-core GEMM per modulus.  Double and
+ * complex double; float runs BF16x3 and complex float the native kernel, as
+ * under COSMA_GPU_METHOD_OZAKI. */
+#define COSMA_GPU_METHOD_OZAKI2 4
 
 /* Statistics of one Ozaki-split GEMM (filled when a non-null pointer is
  * given). */
@@ -72,6 +77,7 @@ typedef struct cosma_gpu_ozaki_info {
     double spread_bits;  /* exponent-spread estimate used to size slices    */
     double prep_ms;      /* scaling + slicing kernels (CUDA events)         */
     double gemm_ms;      /* slice-product GEMM kernel (CUDA events)         */
+    int fraction_bits;   /* fixed-point fraction bits of the operands       */
 } cosma_gpu_ozaki_info;
 
 /* ----------------------------------------------------- Tiled-MM interface */
@@ -184,6 +190,37 @@ int cosma_gpu_zgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n,
                                  const double* alpha, const double* A, int64_t lda,
                                  const double* B, int64_t ldb, const double* beta, double* C,
                                  int64_t ldc, int slices, void* stream, cosma_gpu_ozaki_info* info);
+
+/* FP64-accurate DGEMM by the Chinese-remainder form of the Ozaki scheme
+ * (Ozaki scheme II; new, no reference counterpart).  op(A) and op(B) are
+ * scaled per row / column by powers of two and rounded to integers of P
+ * fraction bits; their residues modulo `moduli` pairwise coprime moduli
+ * <= 255 are multiplied exactly on the BF16 tensor cores (one GEMM per
+ * modulus), and the exact integer product is rebuilt by the Chinese
+ * remainder theorem and rounded once to FP64.  moduli <= 0 sizes the count
+ * (and P) from the inputs' exponent spread; explicit counts run from 2 to
+ * 28, and P is the largest the count allows for this k.  In *info,
+ * `slices` and `products` report the modulus count, `groups` the FP32
+ * accumulator drains per output tile, `fraction_bits` P.  Inf/NaN inputs
+ * run the native kernel (fallback_native = 1).  k beyond 4,194,240 runs in
+ * passes accumulated through C. */
+int cosma_gpu_dgemm_ozaki2_device(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                  double alpha, const double* A, int64_t lda, const double* B,
+                                  int64_t ldb, double beta, double* C, int64_t ldc, int moduli,
+                                  void* stream, cosma_gpu_ozaki_info* info);
+/* The modulus count and fraction bits P that cosma_gpu_dgemm_ozaki2_device
+ * uses for depth k (2k for the complex form) and the measured exponent
+ * spread of the operands (the info record's spread_bits); moduli > 0 fixes
+ * the count as in the GEMM call.  Host-only: touches no device. */
+int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int moduli, int* nmod, int* fraction_bits);
+/* The same for complex double (interleaved re/im, op N, T or C): both parts
+ * of C come out of one modular GEMM of depth 2k per modulus (four real
+ * products per complex one), each part exact before its one rounding.
+ * alpha/beta point to {re, im}. */
+int cosma_gpu_zgemm_ozaki2_device(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                  const double* alpha, const double* A, int64_t lda,
+                                  const double* B, int64_t ldb, const double* beta, double* C,
+                                  int64_t ldc, int moduli, void* stream, cosma_gpu_ozaki_info* info);
 
 /* Size of the static device array that cosma_gpu_dgemm_ozaki_noalloc draws
  * all of its scratch from (64 MiB, held on every GPU that loads the library). */

@@ -1,0 +1,163 @@
+"""Chinese-remainder (Ozaki scheme II) FP64-accurate GEMM vs the oracle.
+
+* bit-exact against the CPU restatement (oracle/ozaki2.py: the exact integer
+  product of the rounded operands, rounded once) on small sizes, every op
+  combination, explicit and automatic modulus counts;
+* K beyond one exact FP32 accumulation (1024) and beyond the 64-chunk
+  reduction of the 32-bit running sums;
+* several tiles per CTA pair (persistent loop over (modulus, tile) units) on
+  sampled entries;
+* alpha and beta, beta == 0 with NaN in C, non-finite inputs (native path);
+* the complex form (four real products per complex one), ops N/T/C;
+* accuracy against the double-double oracle for the precision
+  configuration's distributions.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import from_dev, to_dev
+from oracle import ozaki2 as o2
+
+pytestmark = pytest.mark.gpu
+
+
+def _op_shape(op, m, k):
+    return (m, k) if op == "N" else (k, m)
+
+
+def _run(ta, tb, m, n, k, A, B, alpha=1.0, beta=0.0, C0=None, moduli=0, lda=None, ldb=None, ldc=None):
+    from cosma_gb300 import dgemm_ozaki2_device
+    lda = lda or A.shape[0]
+    ldb = ldb or B.shape[0]
+    ldc = ldc or m
+    dA, dB = to_dev(A, lda), to_dev(B, ldb)
+    dC = to_dev(C0 if C0 is not None else np.zeros((m, n)), ldc)
+    info = dgemm_ozaki2_device(ta, tb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, moduli=moduli)
+    return from_dev(dC, m, n, ldc), info
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T"), ("T", "T")])
+@pytest.mark.parametrize("m,n,k,N", [(17, 9, 33, 6), (64, 40, 130, 12), (130, 70, 200, 18), (5, 300, 129, 28)])
+def test_bit_exact_against_restatement(native_lib, cuda, ta, tb, m, n, k, N):
+    A = oracle.exp_spread(_op_shape(ta, m, k), m + k, 6)
+    B = oracle.exp_spread(_op_shape(tb, k, n), n + k, 6)
+    got, info = _run(ta, tb, m, n, k, A, B, moduli=N, lda=A.shape[0] + 1, ldc=m + 3)
+    P = o2.max_fraction_bits(N, k)
+    assert info["slices"] == N and info["fraction_bits"] == P
+    np.testing.assert_array_equal(got, o2.ozaki2_gemm(ta, tb, A, B, P))
+
+
+def test_automatic_modulus_count(native_lib, cuda):
+    import cosma_gb300 as cg
+    m, n, k = 48, 40, 300
+    for phi in (0, 8, 32):
+        A = oracle.exp_spread((m, k), 10 + phi, phi)
+        B = oracle.exp_spread((k, n), 20 + phi, phi)
+        got, info = _run("N", "N", m, n, k, A, B)
+        assert (info["slices"], info["fraction_bits"]) == cg.ozaki2_choose(k, info["spread_bits"])
+        np.testing.assert_array_equal(got, o2.ozaki2_gemm("N", "N", A, B, info["fraction_bits"]))
+
+
+@pytest.mark.parametrize("k", [1024, 1025, 5000, 70000])
+def test_long_k_chunks_and_reductions(native_lib, cuda, k):
+    """1024 products per exact accumulation; 64 chunks per running-sum reduction."""
+    m, n = 9, 7
+    A = oracle.uniform((m, k), k)
+    B = oracle.uniform((k, n), k + 1)
+    got, info = _run("N", "N", m, n, k, A, B, moduli=18)
+    assert info["groups"] == 18 * -(-k // 1024)
+    np.testing.assert_array_equal(got, o2.ozaki2_gemm("N", "N", A, B, info["fraction_bits"]))
+
+
+def test_exact_integer_product_at_maximal_residues(native_lib, cuda):
+    """Integer inputs are represented exactly, so C is the exact integer product;
+    rows / columns of maximal magnitude stress the 2^24 accumulator bound."""
+    rng = np.random.default_rng(3)
+    m, n, k = 256, 256, 4096
+    A = np.asfortranarray(rng.integers(-2 ** 20, 2 ** 20, (m, k)).astype(np.float64))
+    B = np.asfortranarray(rng.integers(-2 ** 20, 2 ** 20, (k, n)).astype(np.float64))
+    A[:4, :] = 2.0 ** 20 - 1
+    B[:, :4] = -(2.0 ** 20 - 1)
+    got, info = _run("N", "N", m, n, k, A, B, moduli=20)
+    exact = A.astype(np.int64) @ B.astype(np.int64)  # |sum| < 2^52: exact in int64 and in double
+    np.testing.assert_array_equal(got, exact.astype(np.float64))
+
+
+@pytest.mark.parametrize("ta,tb,m,n,k,N", [
+    ("N", "N", 2560, 2304, 256, 8),   # 90 pair tiles x 8 moduli over 76 pairs
+    ("T", "N", 1300, 700, 300, 18),   # m padded to 1536
+    ("N", "T", 384, 5120, 200, 12),
+])
+def test_bit_exact_sampled_many_tiles(native_lib, cuda, ta, tb, m, n, k, N):
+    A = oracle.exp_spread(_op_shape(ta, m, k), m + 3, 6)
+    B = oracle.exp_spread(_op_shape(tb, k, n), n + 5, 6)
+    got, info = _run(ta, tb, m, n, k, A, B, moduli=N)
+    rng = np.random.default_rng(m + n)
+    rows = np.concatenate([rng.integers(0, m, 600), [0, m - 1, m - 1, 0]])
+    cols = np.concatenate([rng.integers(0, n, 600), [0, n - 1, 0, n - 1]])
+    ref = o2.ozaki2_gemm_sampled(ta, tb, A, B, info["fraction_bits"], rows, cols)
+    np.testing.assert_array_equal(got[rows, cols], ref)
+
+
+def test_alpha_beta_and_nan_safety(native_lib, cuda):
+    m, n, k = 70, 50, 90
+    A = oracle.uniform((m, k), 1)
+    B = oracle.uniform((k, n), 2)
+    C0 = oracle.uniform((m, n), 3)
+    got, info = _run("N", "N", m, n, k, A, B, alpha=-1.5, beta=0.75, C0=C0, moduli=18)
+    np.testing.assert_array_equal(got, o2.ozaki2_gemm("N", "N", A, B, info["fraction_bits"], -1.5, 0.75, C0))
+    Cnan = np.full((m, n), np.nan)
+    got, info = _run("N", "N", m, n, k, A, B, alpha=2.0, beta=0.0, C0=Cnan, moduli=18)
+    assert not np.isnan(got).any()
+    np.testing.assert_array_equal(got, o2.ozaki2_gemm("N", "N", A, B, info["fraction_bits"], 2.0))
+
+
+def test_non_finite_inputs_run_native(native_lib, cuda):
+    m, n, k = 20, 10, 30
+    A = oracle.uniform((m, k), 4)
+    A[3, 7] = np.inf
+    B = oracle.uniform((k, n), 5)
+    got, info = _run("N", "N", m, n, k, A, B)
+    assert info["fallback_native"] == 1
+    assert np.all(~np.isfinite(got[3])) and np.all(np.isfinite(np.delete(got, 3, axis=0)))
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "C"), ("T", "N"), ("C", "T")])
+def test_complex_bit_exact(native_lib, cuda, ta, tb):
+    from cosma_gb300 import zgemm_ozaki2_device
+    m, n, k, N = 40, 30, 36, 18
+    A = oracle.uniform(_op_shape(ta, m, k), 5, dtype=np.complex128)
+    B = oracle.uniform(_op_shape(tb, k, n), 7, dtype=np.complex128)
+    dA, dB = to_dev(A), to_dev(B)
+    dC = to_dev(np.zeros((m, n), dtype=np.complex128))
+    info = zgemm_ozaki2_device(ta, tb, m, n, k, 1.0, dA, A.shape[0], dB, B.shape[0], 0.0, dC, m, moduli=N)
+    assert info["fraction_bits"] == o2.max_fraction_bits(N, 2 * k)
+    np.testing.assert_array_equal(from_dev(dC, m, n), o2.ozaki2_zgemm(ta, tb, A, B, info["fraction_bits"]))
+
+
+def test_complex_alpha_beta(native_lib, cuda):
+    from cosma_gb300 import zgemm_ozaki2_device
+    m, n, k = 33, 17, 40
+    A = oracle.uniform((m, k), 8, dtype=np.complex128)
+    B = oracle.uniform((k, n), 9, dtype=np.complex128)
+    C0 = oracle.uniform((m, n), 10, dtype=np.complex128)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C0)
+    al, be = 0.5 - 1.25j, 2.0 + 0.5j
+    zgemm_ozaki2_device("N", "N", m, n, k, al, dA, m, dB, k, be, dC, m)
+    exact = A.astype(np.complex256) @ B.astype(np.complex256) if hasattr(np, "complex256") else A @ B
+    want = al * exact.astype(np.complex128) + be * C0
+    np.testing.assert_allclose(from_dev(dC, m, n), want, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("phi", [0, 8, 32])
+def test_accuracy_against_double_double(native_lib, cuda, phi):
+    m = n = 384
+    k = 2048
+    A = oracle.exp_spread((m, k), 40 + phi, phi)
+    B = oracle.exp_spread((k, n), 50 + phi, phi)
+    got, info = _run("N", "N", m, n, k, A, B)
+    hi, lo, ab = oracle.gemm_dd("N", "N", A, B)
+    st = oracle.error_stats(got.ravel(), hi.ravel(), lo.ravel(), ab.ravel())
+    assert st["max_err_over_absab"] <= 2.0 ** -52
+    assert st["max_rel_err"] <= 1e-15, st
