@@ -119,6 +119,8 @@ SIGNATURES = {
     "costa_gpu_unpack_z": (i32, [i64, i64, vp, vp, i64, vp, vp, i64, vp]),
     "costa_gpu_unpack_c": (i32, [i64, i64, vp, vp, i64, vp, vp, i64, vp]),
     "cosma_gpu_pxgemm_set_method": (i32, [i32]),
+    "cosma_gpu_test_fail_next": (i32, [i32, i32]),
+    "cosma_gpu_test_faults_pending": (i32, [i32]),
     "cosma_gpu_host_copy_route": (i32, [vp]),
 }
 for _pre in ("p", "P", "cosma_p", "COSMA_P"):

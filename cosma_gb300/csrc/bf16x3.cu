@@ -271,11 +271,10 @@ Workspace* workspace(cudaStream_t s) {
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lock(g_mu);
     auto& w = g_ws[{dev, s}];
-    if (!w) {
-        w = new Workspace();
-        if (cudaMallocHost(&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
-        cudaGetLastError();
-    }
+    if (!w) w = new Workspace();
+    // (re)tried until it exists: a failed allocation fails this call only
+    if (!w->host_err && pinned_alloc((void**)&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
+    cudaGetLastError();
     return w;
 }
 

@@ -10,11 +10,12 @@ int DeviceBuffer::reserve(size_t need, cudaStream_t stream) {
     // 2 MiB granularity keeps small size changes from reallocating.
     size_t rounded = (need + (2u << 20) - 1) & ~size_t((2u << 20) - 1);
     (void)stream;
-    cudaError_t e = cudaMalloc(&ptr, rounded);
+    const bool injected = inject_fault(kFaultDeviceAlloc);
+    cudaError_t e = injected ? cudaErrorMemoryAllocation : cudaMalloc(&ptr, rounded);
     if (e != cudaSuccess) {
         ptr = nullptr;
         bytes = 0;
-        return cuda_status(e, "cudaMalloc(workspace)");
+        return cuda_status(e, injected ? "cudaMalloc(workspace) [injected fault]" : "cudaMalloc(workspace)");
     }
     bytes = rounded;
     return COSMA_GPU_SUCCESS;

@@ -36,11 +36,19 @@ struct Stager {
 std::mutex g_stage_mu;
 Stager g_stager;  // one per process: the copies below hold g_stage_mu
 
+// Allocates what is still missing; a failure leaves the copies on the
+// driver's own pageable path and is retried by the next copy.
 bool stager_ready() {
     if (g_stager.ok) return true;
     for (int i = 0; i < 2; ++i) {
-        if (cudaMallocHost(&g_stager.buf[i], kStageBytes) != cudaSuccess) { g_stager.buf[i] = nullptr; break; }
-        if (cudaEventCreateWithFlags(&g_stager.done[i], cudaEventDisableTiming) != cudaSuccess) break;
+        if (!g_stager.buf[i] && pinned_alloc(&g_stager.buf[i], kStageBytes) != cudaSuccess) {
+            g_stager.buf[i] = nullptr;
+            break;
+        }
+        if (!g_stager.done[i] && cudaEventCreateWithFlags(&g_stager.done[i], cudaEventDisableTiming) != cudaSuccess) {
+            g_stager.done[i] = nullptr;
+            break;
+        }
     }
     cudaGetLastError();
     g_stager.ok = g_stager.buf[0] && g_stager.buf[1] && g_stager.done[0] && g_stager.done[1];

@@ -534,14 +534,14 @@ Workspace* workspace(cudaStream_t s) {
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lock(g_ws_mu);
     auto& w = g_ws[{dev, s}];
-    if (!w) {
-        w = new Workspace();
-        if (cudaMallocHost(&w->host_stats, sizeof(Stats)) != cudaSuccess) w->host_stats = nullptr;
-        if (cudaMallocHost(&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
-        for (auto& e : w->ev)
-            if (cudaEventCreate(&e) != cudaSuccess) e = nullptr;
-        cudaGetLastError();
-    }
+    if (!w) w = new Workspace();
+    // pinned staging and events, (re)tried until they exist: a failed
+    // allocation fails this call only
+    if (!w->host_stats && pinned_alloc((void**)&w->host_stats, sizeof(Stats)) != cudaSuccess) w->host_stats = nullptr;
+    if (!w->host_err && pinned_alloc((void**)&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
+    for (auto& e : w->ev)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) e = nullptr;
+    cudaGetLastError();
     return w;
 }
 

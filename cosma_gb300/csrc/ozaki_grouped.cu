@@ -587,8 +587,8 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
     pl->orig.assign(in, in + count);
     pl->hp.assign(count, Prob{});
     CGB_CUDA(cudaStreamCreateWithFlags(&pl->cs, cudaStreamNonBlocking));
-    if (cudaMallocHost(&pl->host_bad, sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(&pl->host_err, sizeof(unsigned)) != cudaSuccess)
+    if (pinned_alloc((void**)&pl->host_bad, sizeof(int)) != cudaSuccess ||
+        pinned_alloc((void**)&pl->host_err, sizeof(unsigned)) != cudaSuccess)
         return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "grouped ozaki: pinned staging");
 
     // 1. normalise; exponent arena offsets; scaling items

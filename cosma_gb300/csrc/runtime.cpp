@@ -7,6 +7,7 @@
 #include "runtime.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cstdlib>
 #include <string>
@@ -66,6 +67,26 @@ int default_tile_n() { return (int)env_ll("COSMA_GPU_MAX_TILE_N", 32768); }
 int default_tile_k() { return (int)env_ll("COSMA_GPU_MAX_TILE_K", 32768); }
 bool default_pinning() { return env_bool("COSMA_GPU_MEMORY_PINNING", true); }
 
+namespace {
+std::atomic<int> g_faults[kFaultSites];
+}  // namespace
+
+bool inject_fault(int site) {
+    if (site <= 0 || site >= kFaultSites) return false;
+    int v = g_faults[site].load();
+    while (v > 0)
+        if (g_faults[site].compare_exchange_weak(v, v - 1)) return true;
+    return false;
+}
+
+cudaError_t pinned_alloc(void** p, size_t bytes) {
+    if (inject_fault(kFaultPinnedAlloc)) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMallocHost(p, bytes);
+}
+
 int device_sm_count() {
     static PerDevice<int> cache;
     int n = kNumSMs;
@@ -100,6 +121,19 @@ int default_method() {
 extern "C" {
 
 int cosma_gpu_last_error(void) { return cgb::t_last_code; }
+
+int cosma_gpu_test_fail_next(int site, int count) {
+    cgb::clear_error();
+    if (site <= 0 || site >= cgb::kFaultSites || count < 0)
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "test_fail_next: site 1..3 and count >= 0");
+    cgb::g_faults[site].store(count);
+    return COSMA_GPU_SUCCESS;
+}
+
+int cosma_gpu_test_faults_pending(int site) {
+    if (site <= 0 || site >= cgb::kFaultSites) return -1;
+    return cgb::g_faults[site].load();
+}
 
 const char* cosma_gpu_last_error_string(void) { return cgb::t_last_msg.c_str(); }
 

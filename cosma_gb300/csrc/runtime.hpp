@@ -58,6 +58,14 @@ class PerDevice {
     T val_[kMaxDevices] = {};
 };
 
+// Host-side fault injection for tests (cosma_gpu_test_fail_next): each call
+// at an armed site consumes one pending fault and reports it, so the caller
+// takes its error path as if the CUDA call had failed.  No GPU is involved.
+enum FaultSite { kFaultDeviceAlloc = 1, kFaultHostRegister = 2, kFaultPinnedAlloc = 3, kFaultSites = 4 };
+bool inject_fault(int site);
+// cudaMallocHost behind the kFaultPinnedAlloc site.
+cudaError_t pinned_alloc(void** p, size_t bytes);
+
 // SM count of the current device (cached per device; 152 if the query fails).
 int device_sm_count();
 

@@ -87,7 +87,8 @@ int pin_range(cosma_gpu_mm_handle* h, const void* ptr, size_t bytes, std::vector
             h->pinned.erase(it);
         }
     }
-    cudaError_t e = cudaHostRegister((void*)ptr, bytes, cudaHostRegisterDefault);
+    cudaError_t e =
+        inject_fault(kFaultHostRegister) ? cudaErrorMemoryAllocation : cudaHostRegister((void*)ptr, bytes, cudaHostRegisterDefault);
     if (e == cudaErrorHostMemoryAlreadyRegistered) {  // page-locked by its owner
         cudaGetLastError();
         return COSMA_GPU_SUCCESS;

@@ -250,6 +250,23 @@ int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m, int64_t n
                                   int64_t ldb, double beta, double* C, int64_t ldc, int slices,
                                   void* stream, cosma_gpu_ozaki_info* info);
 
+/* ----------------------------------------------------- fault injection */
+/* Test hook (new; the reference has none): the next `count` calls at `site`
+ * fail on the host as if CUDA had refused them, so that callers can check the
+ * error paths without faulting a GPU.  Sites: 1 device workspace allocation
+ * (cudaMalloc: the call returns COSMA_GPU_ERROR_OUT_OF_MEMORY with a message),
+ * 2 page-locking of caller memory (cudaHostRegister: the streamer falls back
+ * to its unregistered copy route, same result), 3 pinned staging allocations
+ * (cudaMallocHost: an Ozaki / 3xBF16 call returns OUT_OF_MEMORY, the host
+ * copies fall back to the driver's pageable copies).  count 0 disarms the
+ * site.  Handles and contexts stay usable after an injected failure. */
+#define COSMA_GPU_FAULT_DEVICE_ALLOC 1
+#define COSMA_GPU_FAULT_HOST_REGISTER 2
+#define COSMA_GPU_FAULT_PINNED_ALLOC 3
+int cosma_gpu_test_fail_next(int site, int count);
+/* Faults still armed at `site` (-1 for an unknown site). */
+int cosma_gpu_test_faults_pending(int site);
+
 /* ------------------------------------------------- grouped (batched) GEMM */
 /* One problem of a batch: C = alpha * op(A) * op(B) + beta * C on device
  * pointers (column-major).  Layout is part of the ABI (80 bytes). */
