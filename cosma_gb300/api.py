@@ -270,6 +270,17 @@ def zgemm_ozaki2_device(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, Cm
     return info.as_dict()
 
 
+def dgemm_ozaki2_residual(transa, transb, m, n, k, A, lda, B, ldb, Ct, ldt, E, Rx, ldo, moduli=28, stream=None):
+    """E = op(A) op(B) - Ct (exact before one rounding) and Rx = op(A) op(B)
+    rounded once, on CUDA buffers; returns the statistics."""
+    lib = N.load()
+    info = N.OzakiInfo()
+    N.check(lib.cosma_gpu_dgemm_ozaki2_residual(transa.encode(), transb.encode(), m, n, k, ptr(A), lda, ptr(B), ldb,
+                                                ptr(Ct), ldt, moduli, ptr(E), ptr(Rx), ldo, _stream_ptr(stream),
+                                                C.byref(info)))
+    return info.as_dict()
+
+
 def ozaki2_choose(k, spread_bits=0.0, moduli=0):
     """(modulus count, fraction bits P) the Chinese-remainder form uses (host only)."""
     lib = N.load()

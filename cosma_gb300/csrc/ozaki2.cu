@@ -89,81 +89,83 @@ __device__ __forceinline__ uint32_t mod32(uint32_t u, uint32_t p, uint32_t magic
     return r >= p ? r - p : r;
 }
 
+constexpr int LIMB18 = 7;  // 18-bit limbs of a scaled integer (P <= 120: at most 121 bits)
+
 struct SplitParams {
     int nmod;
-    int P;  // fraction bits
-    uint32_t p[MAX_MODULI], magic[MAX_MODULI], c32[MAX_MODULI];  // c32 = 2^32 mod p
+    int P;      // fraction bits
+    int limbs;  // 18-bit limbs the scaled integers need: ceil((P + 1) / 18)
+    uint32_t p[MAX_MODULI], magic[MAX_MODULI];
+    uint32_t c18[MAX_MODULI][LIMB18];  // 2^(18 i) mod p
 };
 
-struct RowInt {  // |x| 2^(P - E) rounded = (mhi:mlo) * 2^sh, 0 <= sh < 128
-    uint32_t mlo, mhi;
-    int sh;
+// The scaled integer X = round_half_away(|x| 2^(P - E)) of one operand
+// element as 18-bit limbs (X < 2^(P+1)), with its sign.  |x| = M 2^eu with
+// the 53-bit significand M; X = M 2^sh exactly when sh >= 0.
+struct Scaled {
+    uint32_t d[LIMB18];
     bool neg;
 };
 
-__device__ __forceinline__ RowInt scaled_integer(double x, int E, int P) {
+__device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    RowInt v;
+    Scaled v;
     v.neg = (b >> 63) != 0;
     const int ef = (int)((b >> 52) & 0x7FF);
     unsigned long long M = b & 0xFFFFFFFFFFFFFull;
     int eu;
     if (ef == 0) eu = -1074; else { M |= 1ull << 52; eu = ef - 1075; }
-    int sh = eu - E + P;
+    int sh = eu - E + P;  // < P: |x| < 2^E
     if (M == 0) sh = 0;
     if (sh < 0) {  // round half away from zero
         const int r = -sh;
         M = r > 63 ? 0ull : (M + (1ull << (r - 1))) >> r;
         sh = 0;
     }
-    v.mlo = (uint32_t)M;
-    v.mhi = (uint32_t)(M >> 32);
-    v.sh = sh;
+    // X = M << sh as a 128-bit integer (hi:lo), then cut into 18-bit limbs
+    unsigned long long lo, hi;
+    if (sh == 0) { lo = M; hi = 0; }
+    else if (sh < 64) { lo = M << sh; hi = M >> (64 - sh); }
+    else { lo = 0; hi = M << (sh - 64); }
+#pragma unroll
+    for (int i = 0; i < LIMB18; ++i) {
+        const int pos = 18 * i;
+        unsigned long long w;
+        if (pos + 18 <= 64) w = lo >> pos;
+        else if (pos >= 64) w = hi >> (pos - 64);
+        else w = (lo >> pos) | (hi << (64 - pos));
+        v.d[i] = (uint32_t)w & 0x3FFFFu;
+    }
     return v;
 }
 
-// Balanced residue of the scaled integer modulo p: in [-(p-1)/2, p/2] (p odd),
-// [-126, 127] for p = 254.
-__device__ __forceinline__ int balanced_residue(const RowInt& v, uint32_t p, uint32_t magic, uint32_t c32,
-                                                uint32_t pow2) {
-    uint32_t r = mod32(v.mlo, p, magic);
-    r = mod32(v.mhi * c32 + r, p, magic);  // mhi < 2^21, c32 < 2^8
-    r = mod32(r * pow2, p, magic);         // < 2^16
-    int s = (int)r;
+// Balanced residue of X modulo p, sign applied: sum_i d_i (2^(18 i) mod p) is
+// below 7 * 2^18 * 2^8 < 2^29, so one reduction finishes it.  The result lies
+// in [-(p-1)/2, p/2] ([-126, 127] for p = 254) before the sign.
+template <int NL>
+__device__ __forceinline__ int balanced_residue(const Scaled& v, uint32_t p, uint32_t magic, const uint32_t* c18) {
+    uint32_t u = v.d[0];
+#pragma unroll
+    for (int i = 1; i < NL; ++i) u += v.d[i] * c18[i];
+    int s = (int)mod32(u, p, magic);
     if (s > (int)(p >> 1)) s -= (int)p;
     return v.neg ? -s : s;
 }
 
-__device__ __forceinline__ uint32_t bf16_bits(int v) {
-    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn((float)v));
-}
-
-// 2^s mod p for s < 128 and every modulus, in shared memory.
-__device__ __forceinline__ void fill_pow2(uint8_t (*pow2)[128], const SplitParams& sp) {
-    for (int idx = threadIdx.x; idx < sp.nmod * 128; idx += blockDim.x) {
-        const int t = idx >> 7, s = idx & 127;
-        const uint32_t p = sp.p[t], mg = sp.magic[t];
-        uint32_t r = 1 % p, base = 2 % p;
-        for (int e = s; e; e >>= 1) {
-            if (e & 1) r = mod32(r * base, p, mg);
-            base = mod32(base * base, p, mg);
-        }
-        pow2[t][s] = (uint8_t)r;
-    }
-}
+// BF16 bits of a small integer (|v| <= 256): the upper half of its FP32 bits,
+// exact because the value needs at most 8 significant bits.
+__device__ __forceinline__ uint32_t bf16_bits(int v) { return __float_as_uint((float)v) >> 16; }
 
 // Residue matrices of a real (rows x k) operand: N BF16 matrices [t][rows_pad][k_pad],
 // zero padded.  A block of 256 threads covers 32 rows x 64 K elements, each
 // thread 8 consecutive K elements of one row (one 16-byte store per modulus).
-// kcontig: element (r, l) at X[l + r*ld], else at X[r + l*ld].
-template <bool KCONTIG>
+// kcontig: element (r, l) at X[l + r*ld], else at X[r + l*ld].  NL: 18-bit
+// limbs of the scaled integers.
+template <bool KCONTIG, int NL>
 __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows,
                                                     int64_t k, const int* __restrict__ exps, int64_t k_pad,
                                                     int64_t rows_pad, uint16_t* __restrict__ out,
                                                     const __grid_constant__ SplitParams sp) {
-    __shared__ uint8_t pow2[MAX_MODULI][128];
-    fill_pow2(pow2, sp);
-    __syncthreads();
     const int t = threadIdx.x;
     int64_t r;
     int kc;
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
     const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 8;
     if (r >= rows_pad || l0 >= k_pad) return;
     const int E = r < rows ? exps[r] : 0;
-    RowInt v[8];
+    Scaled v[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
         const int64_t l = l0 + e;
@@ -184,12 +186,12 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
     const int64_t slab = rows_pad * k_pad;
 #pragma unroll 1
     for (int m = 0; m < sp.nmod; ++m) {
-        const uint32_t p = sp.p[m], mg = sp.magic[m], c = sp.c32[m];
+        const uint32_t p = sp.p[m], mg = sp.magic[m];
         uint32_t w[4];
 #pragma unroll
         for (int e = 0; e < 8; e += 2) {
-            const uint32_t lo = bf16_bits(balanced_residue(v[e], p, mg, c, pow2[m][v[e].sh]));
-            const uint32_t hi = bf16_bits(balanced_residue(v[e + 1], p, mg, c, pow2[m][v[e + 1].sh]));
+            const uint32_t lo = bf16_bits(balanced_residue<NL>(v[e], p, mg, sp.c18[m]));
+            const uint32_t hi = bf16_bits(balanced_residue<NL>(v[e + 1], p, mg, sp.c18[m]));
             w[e / 2] = lo | (hi << 16);
         }
         *reinterpret_cast<uint4*>(o + m * slab) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -205,15 +207,12 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
 // of the negated integer, so the signs are applied to the residues.  kh is k
 // padded to 64; the row pitch is 2*kh; modulus t starts at t * slice_rows *
 // 2*kh.  X holds interleaved complex doubles, ld in complex elements.
-template <bool KCONTIG, bool BSIDE>
+template <bool KCONTIG, bool BSIDE, int NL>
 __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restrict__ X, int64_t ld, int64_t rows,
                                                          int64_t k, const int* __restrict__ exps, int64_t kh,
                                                          int64_t rows_pad, int64_t slice_rows, int conj,
                                                          uint16_t* __restrict__ out,
                                                          const __grid_constant__ SplitParams sp) {
-    __shared__ uint8_t pow2[MAX_MODULI][128];
-    fill_pow2(pow2, sp);
-    __syncthreads();
     const int t = threadIdx.x;
     int64_t r;
     int kc;
@@ -226,7 +225,7 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
     const double* Xd = reinterpret_cast<const double*>(X);
 #pragma unroll 1
     for (int part = 0; part < 2; ++part) {
-        RowInt v[8];
+        Scaled v[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             const int64_t l = l0 + e;
@@ -237,12 +236,12 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
         }
 #pragma unroll 1
         for (int m = 0; m < sp.nmod; ++m) {
-            const uint32_t p = sp.p[m], mg = sp.magic[m], c = sp.c32[m];
+            const uint32_t p = sp.p[m], mg = sp.magic[m];
             uint32_t w[4], nw[4];
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
-                const int a = balanced_residue(v[e], p, mg, c, pow2[m][v[e].sh]);
-                const int b = balanced_residue(v[e + 1], p, mg, c, pow2[m][v[e + 1].sh]);
+                const int a = balanced_residue<NL>(v[e], p, mg, sp.c18[m]);
+                const int b = balanced_residue<NL>(v[e + 1], p, mg, sp.c18[m]);
                 w[e / 2] = bf16_bits(a) | (bf16_bits(b) << 16);
                 nw[e / 2] = bf16_bits(-a) | (bf16_bits(-b) << 16);
             }
@@ -474,6 +473,11 @@ struct CombineParams {
     double* C;
     double alpha, beta;
     int alpha_one, beta_zero;
+    // residual mode (real only): E = V 2^e - Ct exactly rounded, Rx = V 2^e rounded
+    const double* Ct;
+    int64_t ldt, ldo;
+    double* E;
+    double* Rx;
 };
 
 // Bits [s, s + 64) of the L-limb integer x (static limb indices only).
@@ -535,12 +539,43 @@ __device__ __forceinline__ int cmp_limbs(const uint32_t (&x)[L], const uint32_t*
     return c;
 }
 
+// |x| * 2^e2 rounded once to FP64 (round to nearest even), negated if neg:
+// the top 127 bits with the bits below folded into a sticky last bit (below
+// the rounding position whenever bits were dropped, so the rounding is
+// unaffected); bit 127 of the window stays clear, it is the converter's sign.
+template <int L>
+__device__ __forceinline__ double limbs_to_double(const uint32_t (&x)[L], bool neg, int e2) {
+    int top = -1;
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+        if (x[l]) top = 32 * l + 31 - __clz((int)x[l]);
+    if (top < 0) return 0.0;
+    const int b0 = top > 126 ? top - 126 : 0;
+    unsigned long long lo = bits64<L>(x, b0), hi = bits64<L>(x, b0 + 64);
+    if (b0 > 0 && any_below<L>(x, b0)) lo |= 1ull;
+    const double r = oz::i128_to_double(lo, hi, e2 + b0);
+    return neg ? -r : r;
+}
+
+// x = m << s as limbs (m < 2^53, s + 53 <= 32 L).
+template <int L>
+__device__ __forceinline__ void set_shifted(uint32_t (&x)[L], unsigned long long m, int s) {
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        const int pos = s - 32 * l;  // where bit 0 of m lands relative to limb l
+        uint32_t v = 0;
+        if (pos >= 0 && pos < 32) v = (uint32_t)(m << pos);
+        else if (pos < 0 && pos > -64) v = (uint32_t)(m >> -pos);
+        x[l] = v;
+    }
+}
+
 // One output element per thread: a block of 16 warps covers 32 rows x 16
 // GEMM columns (block b: row block b % row_blocks, column block b /
 // row_blocks); warp w takes column 16*cb + w, lane the row 32*rb + lane, so
 // that the 16 warps read the 512 contiguous residue bytes of each modulus
 // together.
-template <int L>
+template <int L, bool RESIDUAL>
 __global__ void __launch_bounds__(512) combine_kernel(const __grid_constant__ CombineParams p) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t rb = (int64_t)blockIdx.x % p.row_blocks, cb = (int64_t)blockIdx.x / p.row_blocks;
@@ -598,21 +633,47 @@ __global__ void __launch_bounds__(512) combine_kernel(const __grid_constant__ Co
 #pragma unroll
         for (int l = 0; l < L; ++l) x[l] = y[l];
     }
-    // round |V| * 2^(E_i + F_j - 2P) once to FP64: the top 127 bits with the
-    // bits below folded into a sticky last bit (below the rounding position
-    // whenever bits were dropped, so round-to-nearest-even is unaffected)
-    int top = -1;
+    // V * 2^(E_i + F_j - 2P), rounded once
+    const int e2 = p.expA[i] + p.expB[j] - p.twoP;
+    double r = limbs_to_double<L>(x, neg, e2);
+    if constexpr (RESIDUAL) {
+        // T = Ct * 2^-e2 is an integer whenever Ct's last bit weighs at least
+        // 2^e2 (always, but for a Ct below ~2^(e2 + 52)); then E = (V - T)
+        // 2^e2 is exact before its one rounding.  Otherwise E is NaN.
+        const double ct = p.Ct[i + j * p.ldt];
+        const unsigned long long b = (unsigned long long)__double_as_longlong(ct);
+        const bool cneg = (b >> 63) != 0;
+        const int ef = (int)((b >> 52) & 0x7FF);
+        unsigned long long mc = b & 0xFFFFFFFFFFFFFull;
+        int ec;
+        if (ef == 0) ec = -1074; else { mc |= 1ull << 52; ec = ef - 1075; }
+        const int s = ec - e2;
+        double err;
+        if (ef == 0x7FF || (mc && (s < 0 || s + 53 > 32 * L - 1))) {
+            err = __longlong_as_double(0x7FF8000000000000ll);
+        } else {
+            uint32_t t[L];
+            set_shifted<L>(t, mc, mc ? s : 0);
+            bool dneg;
+            if (neg == cneg) {  // |V - T| = ||V| - |T||
+                if (cmp_limbs<L>(x, t) >= 0) {
+                    sub_limbs<L>(x, t);
+                    dneg = neg;
+                } else {
+                    sub_limbs<L>(t, x);
 #pragma unroll
-    for (int l = 0; l < L; ++l)
-        if (x[l]) top = 32 * l + 31 - __clz((int)x[l]);
-    double r = 0.0;
-    if (top >= 0) {
-        const int e2 = p.expA[i] + p.expB[j] - p.twoP;
-        const int b0 = top > 126 ? top - 126 : 0;  // bit 127 of the window stays clear: it is the sign
-        unsigned long long lo = bits64<L>(x, b0), hi = bits64<L>(x, b0 + 64);
-        if (b0 > 0 && any_below<L>(x, b0)) lo |= 1ull;
-        r = oz::i128_to_double(lo, hi, e2 + b0);
-        if (neg) r = -r;
+                    for (int l = 0; l < L; ++l) x[l] = t[l];
+                    dneg = !neg;
+                }
+            } else {  // |V - T| = |V| + |T|
+                add_limbs<L>(x, t);
+                dneg = neg;
+            }
+            err = limbs_to_double<L>(x, dneg, e2);
+        }
+        p.E[i + j * p.ldo] = err;
+        p.Rx[i + j * p.ldo] = r;
+        return;
     }
     double* cp = p.C + (i + j * p.ldc) * p.cs + part;
     if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
@@ -713,11 +774,16 @@ void fill_split(SplitParams& sp, int nmod, int P) {
     std::memset(&sp, 0, sizeof(sp));
     sp.nmod = nmod;
     sp.P = P;
+    sp.limbs = (P + 1 + 17) / 18;
     for (int t = 0; t < nmod; ++t) {
         const uint32_t p = kModuli[t];
         sp.p[t] = p;
         sp.magic[t] = (uint32_t)((1ull << 32) / p);
-        sp.c32[t] = (uint32_t)((1ull << 32) % p);
+        unsigned long long c = 1;
+        for (int i = 0; i < LIMB18; ++i) {
+            sp.c18[t][i] = (uint32_t)c;
+            c = (c << 18) % p;
+        }
     }
 }
 
@@ -739,6 +805,57 @@ void fill_combine(CombineParams& cp, int nmod, int P) {
     for (int l = 0; l < LIMBS; ++l) cp.halfM[l] = (M.w[l] >> 1) | (l + 1 < LIMBS ? (M.w[l + 1] << 31) : 0u);
     cp.shift = std::max(0, M.bitlen() - 24);
     cp.inv_mhi = 1.0f / (float)M.bits64(cp.shift);
+}
+
+template <int NL>
+void launch_split_nl(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps,
+                     int64_t k_pad, int64_t rows_pad, uint16_t* out, const SplitParams& sp, dim3 grid,
+                     cudaStream_t st) {
+    if (kcontig) split_kernel<true, NL><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
+    else split_kernel<false, NL><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
+}
+
+void launch_split(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps,
+                  int64_t k_pad, int64_t rows_pad, uint16_t* out, const SplitParams& sp, dim3 grid, cudaStream_t st) {
+    switch (sp.limbs) {  // P <= 71: 4 limbs; <= 89: 5; <= 107: 6; else 7
+        case 1: case 2: case 3: case 4: launch_split_nl<4>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
+        case 5: launch_split_nl<5>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
+        case 6: launch_split_nl<6>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
+        default: launch_split_nl<7>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
+    }
+}
+
+template <int NL>
+void launch_split_cplx_nl(bool kcontig, bool bside, const double2* X, int64_t ld, int64_t rows, int64_t k,
+                          const int* exps, int64_t kh, int64_t rows_pad, int64_t slice_rows, int conj, uint16_t* out,
+                          const SplitParams& sp, dim3 grid, cudaStream_t st) {
+#define CGB_SPLITC(KC, BS) \
+    split_cplx_kernel<KC, BS, NL><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp)
+    if (kcontig) {
+        if (bside) CGB_SPLITC(true, true); else CGB_SPLITC(true, false);
+    } else {
+        if (bside) CGB_SPLITC(false, true); else CGB_SPLITC(false, false);
+    }
+#undef CGB_SPLITC
+}
+
+void launch_split_cplx(bool kcontig, bool bside, const double2* X, int64_t ld, int64_t rows, int64_t k,
+                       const int* exps, int64_t kh, int64_t rows_pad, int64_t slice_rows, int conj, uint16_t* out,
+                       const SplitParams& sp, dim3 grid, cudaStream_t st) {
+    switch (sp.limbs) {
+        case 1: case 2: case 3: case 4:
+            launch_split_cplx_nl<4>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
+            break;
+        case 5:
+            launch_split_cplx_nl<5>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
+            break;
+        case 6:
+            launch_split_cplx_nl<6>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
+            break;
+        default:
+            launch_split_cplx_nl<7>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
+            break;
+    }
 }
 
 // Limbs the reconstruction needs: sum_t r_t w_t < nmod * 255 * M.
@@ -822,18 +939,23 @@ int launch_gemm(const void* resA, const void* resB, int64_t k_pad, const GemmPar
     return COSMA_GPU_SUCCESS;
 }
 
+template <bool RESIDUAL>
+void launch_combine_t(const CombineParams& cp, int limbs, unsigned grid, cudaStream_t st) {
+    switch (limbs) {
+        case 1: case 2: case 3: case 4: combine_kernel<4, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
+        case 5: combine_kernel<5, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
+        case 6: combine_kernel<6, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
+        case 7: combine_kernel<7, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
+        default: combine_kernel<8, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
+    }
+}
+
 int launch_combine(CombineParams& cp, int nmod, int64_t gemm_cols, cudaStream_t st) {
     cp.row_blocks = ceil_div(cp.m, 32);
     const int64_t blocks = cp.row_blocks * ceil_div(gemm_cols, 16);
     if (blocks > 0x7FFFFFFF) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: C too large for the combine grid");
-    const unsigned grid = (unsigned)blocks;
-    switch (limbs_for(nmod)) {
-        case 1: case 2: case 3: case 4: combine_kernel<4><<<grid, 512, 0, st>>>(cp); break;
-        case 5: combine_kernel<5><<<grid, 512, 0, st>>>(cp); break;
-        case 6: combine_kernel<6><<<grid, 512, 0, st>>>(cp); break;
-        case 7: combine_kernel<7><<<grid, 512, 0, st>>>(cp); break;
-        default: combine_kernel<8><<<grid, 512, 0, st>>>(cp); break;
-    }
+    if (cp.E) launch_combine_t<true>(cp, limbs_for(nmod), (unsigned)blocks, st);
+    else launch_combine_t<false>(cp, limbs_for(nmod), (unsigned)blocks, st);
     CGB_CUDA(cudaGetLastError());
     return COSMA_GPU_SUCCESS;
 }
@@ -891,7 +1013,17 @@ int check_device_error(Workspace* w, cudaStream_t st) {
     return COSMA_GPU_SUCCESS;
 }
 
-int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info* info) {
+// Residual mode: instead of writing C, E = op(A) op(B) - Ct (exact before its
+// one rounding) and Rx = op(A) op(B) rounded once, both m x n with ld ldo.
+struct Residual {
+    const double* Ct = nullptr;
+    int64_t ldt = 0;
+    double* E = nullptr;
+    double* Rx = nullptr;
+    int64_t ldo = 0;
+};
+
+int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info* info, const Residual* res = nullptr) {
     const int64_t m = g.m, n = g.n, k = g.k;
     const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
     const double* A = (const double*)g.A;
@@ -920,6 +1052,7 @@ int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
     Plan pl;
     pl.spread = (double)hs.spread[0] + (double)hs.spread[1];
     if (hs.nonfinite) {  // Inf/NaN have no residues: the native FP64 kernel propagates them
+        if (res) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2 residual: A and B must be finite");
         if (info) info->fallback_native = 1;
         return native_gemm(g, st);
     }
@@ -934,12 +1067,8 @@ int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
     {
         dim3 gA((unsigned)(m_pad / 32), (unsigned)(k_pad / 64)), gB((unsigned)(n_pad / 32), (unsigned)(k_pad / 64));
         if (gA.y > 65535 || gB.y > 65535) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: k too large");
-        uint16_t* rA = (uint16_t*)w->resA.ptr;
-        uint16_t* rB = (uint16_t*)w->resB.ptr;
-        if (a_kc) split_kernel<true><<<gA, 256, 0, st>>>(A, g.lda, m, k, (const int*)w->expA.ptr, k_pad, m_pad, rA, sp);
-        else split_kernel<false><<<gA, 256, 0, st>>>(A, g.lda, m, k, (const int*)w->expA.ptr, k_pad, m_pad, rA, sp);
-        if (b_kc) split_kernel<true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, (const int*)w->expB.ptr, k_pad, n_pad, rB, sp);
-        else split_kernel<false><<<gB, 256, 0, st>>>(B, g.ldb, n, k, (const int*)w->expB.ptr, k_pad, n_pad, rB, sp);
+        launch_split(a_kc, A, g.lda, m, k, (const int*)w->expA.ptr, k_pad, m_pad, (uint16_t*)w->resA.ptr, sp, gA, st);
+        launch_split(b_kc, B, g.ldb, n, k, (const int*)w->expB.ptr, k_pad, n_pad, (uint16_t*)w->resB.ptr, sp, gB, st);
         CGB_CUDA(cudaGetLastError());
     }
     CGB_CUDA(cudaEventRecord(w->ev[1], st));
@@ -970,6 +1099,13 @@ int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
     cp.beta = g.beta[0];
     cp.alpha_one = g.alpha[0] == 1.0;
     cp.beta_zero = g.beta[0] == 0.0;
+    if (res) {
+        cp.Ct = res->Ct;
+        cp.ldt = res->ldt;
+        cp.E = res->E;
+        cp.Rx = res->Rx;
+        cp.ldo = res->ldo;
+    }
     CGB_CHECK(launch_combine(cp, pl.nmod, n, st));
     CGB_CHECK(check_device_error(w, st));
     return finish_info(info, w, pl, gp.kb_count);
@@ -1018,13 +1154,10 @@ int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
         if (gA.y > 65535) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: k too large");
         uint16_t* rA = (uint16_t*)w->resA.ptr;
         uint16_t* rB = (uint16_t*)w->resB.ptr;
-        const int ca = g.opa == 2, cb = g.opb == 2;
         const int* eA = (const int*)w->expA.ptr;
         const int* eB = (const int*)w->expB.ptr;
-        if (a_kc) split_cplx_kernel<true, false><<<gA, 256, 0, st>>>(A, g.lda, m, k, eA, kh, m_pad, m_pad, ca, rA, sp);
-        else split_cplx_kernel<false, false><<<gA, 256, 0, st>>>(A, g.lda, m, k, eA, kh, m_pad, m_pad, ca, rA, sp);
-        if (b_kc) split_cplx_kernel<true, true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, eB, kh, nh, n_pad, cb, rB, sp);
-        else split_cplx_kernel<false, true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, eB, kh, nh, n_pad, cb, rB, sp);
+        launch_split_cplx(a_kc, false, A, g.lda, m, k, eA, kh, m_pad, m_pad, g.opa == 2, rA, sp, gA, st);
+        launch_split_cplx(b_kc, true, B, g.ldb, n, k, eB, kh, nh, n_pad, g.opb == 2, rB, sp, gB, st);
         CGB_CUDA(cudaGetLastError());
     }
     CGB_CUDA(cudaEventRecord(w->ev[1], st));
@@ -1073,6 +1206,34 @@ int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
 }  // namespace oz2
 
 }  // namespace cgb
+
+extern "C" int cosma_gpu_dgemm_ozaki2_residual(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                               const double* A, int64_t lda, const double* B, int64_t ldb,
+                                               const double* Ct, int64_t ldt, int moduli, double* E, double* Rx,
+                                               int64_t ldo, void* stream, cosma_gpu_ozaki_info* info) {
+    using namespace cgb;
+    clear_error();
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    const int opa = parse_op(transa), opb = parse_op(transb);
+    if (opa < 0 || opb < 0 || opa == 2 || opb == 2)
+        return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2 residual: op must be N or T");
+    if (m < 1 || n < 1 || k < 1 || k > oz2::KMAX)
+        return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2 residual: 1 <= m, n and 1 <= k <= 4194240");
+    const int64_t a_rows = opa == 0 ? m : k, b_rows = opb == 0 ? k : n;
+    if (lda < a_rows || ldb < b_rows || ldt < m || ldo < m || !A || !B || !Ct || !E || !Rx)
+        return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2 residual: bad pointer or leading dimension");
+    if (((uintptr_t)A | (uintptr_t)B | (uintptr_t)Ct | (uintptr_t)E | (uintptr_t)Rx) % 8)
+        return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2 residual: buffers must be 8-byte aligned");
+    double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
+    GemmDesc g = make_gemm_desc(Scalar::D, transa, transb, m, n, k, one, A, lda, B, ldb, zero, E, ldo);
+    oz2::Residual r;
+    r.Ct = Ct;
+    r.ldt = ldt;
+    r.E = E;
+    r.Rx = Rx;
+    r.ldo = ldo;
+    return oz2::dgemm(g, moduli, (cudaStream_t)stream, info, &r);
+}
 
 extern "C" int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int moduli, int* nmod, int* fraction_bits) {
     cgb::clear_error();

@@ -208,6 +208,19 @@ int cosma_gpu_dgemm_ozaki2_device(char transa, char transb, int64_t m, int64_t n
                                   double alpha, const double* A, int64_t lda, const double* B,
                                   int64_t ldb, double beta, double* C, int64_t ldc, int moduli,
                                   void* stream, cosma_gpu_ozaki_info* info);
+/* Exact residual of a computed product (new; no reference counterpart): for
+ * a candidate Ct (m x n, ld ldt) of op(A) * op(B) (op N or T), writes
+ * E = op(A) op(B) - Ct, exact before its one rounding to FP64, and
+ * Rx = op(A) op(B) rounded once, both m x n with leading dimension ldo.  The
+ * product is the Chinese-remainder form's: exact for operands whose bits all
+ * lie within P fraction bits of their row's / column's leading bit (moduli
+ * = 28 gives P = 98 at k = 16384).  Used to state the error of a result over
+ * every entry; an entry of Ct below ~2^-144 of its row and column scales
+ * gives E = NaN.  k <= 4,194,240, one pass. */
+int cosma_gpu_dgemm_ozaki2_residual(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                                    const double* A, int64_t lda, const double* B, int64_t ldb,
+                                    const double* Ct, int64_t ldt, int moduli, double* E, double* Rx,
+                                    int64_t ldo, void* stream, cosma_gpu_ozaki_info* info);
 /* The modulus count and fraction bits P that cosma_gpu_dgemm_ozaki2_device
  * uses for depth k (2k for the complex form) and the measured exponent
  * spread of the operands (the info record's spread_bits); moduli > 0 fixes

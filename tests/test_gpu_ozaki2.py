@@ -161,3 +161,53 @@ def test_accuracy_against_double_double(native_lib, cuda, phi):
     st = oracle.error_stats(got.ravel(), hi.ravel(), lo.ravel(), ab.ravel())
     assert st["max_err_over_absab"] <= 2.0 ** -52
     assert st["max_rel_err"] <= 1e-15, st
+
+
+def test_residual_mode_is_exact(native_lib, cuda):
+    """E = op(A) op(B) - Ct exact before one rounding, Rx = the product rounded
+    once, against rational arithmetic (every input bit is kept at 28 moduli)."""
+    from fractions import Fraction
+
+    import cosma_gb300 as cg
+    m, n, k = 40, 24, 300
+    A = oracle.uniform((k, m), 61)  # op(A) = A^T
+    B = oracle.uniform((k, n), 62)
+    Ct = np.asfortranarray(A.T @ B)  # a candidate with ordinary FP64 rounding errors
+    Ct[0, 0] = 0.0
+    dA, dB, dCt = to_dev(A), to_dev(B), to_dev(Ct)
+    dE, dR = to_dev(np.zeros((m, n))), to_dev(np.zeros((m, n)))
+    info = cg.dgemm_ozaki2_residual("T", "N", m, n, k, dA, k, dB, k, dCt, m, dE, dR, m, moduli=28)
+    assert info["slices"] == 28 and info["fraction_bits"] >= 98
+    E, R = from_dev(dE, m, n), from_dev(dR, m, n)
+    for i in range(m):
+        for j in range(n):
+            exact = sum(Fraction(float(A[l, i])) * Fraction(float(B[l, j])) for l in range(k))
+            assert R[i, j] == float(exact)
+            assert E[i, j] == float(exact - Fraction(float(Ct[i, j])))
+
+
+def test_full_result_accuracy_at_4096(native_lib, cuda):
+    """Every entry of the 4096^3 precision-configuration product (phi = 0)
+    against the exact product: max elementwise relative error <= 1e-15, and
+    <= 2^-52 of (|A||B|)_ij."""
+    import torch
+
+    import cosma_gb300 as cg
+    n = 4096
+    A = oracle.exp_spread((n, n), 71, 0)
+    B = oracle.exp_spread((n, n), 72, 0)
+    dA = torch.from_numpy(A.reshape(-1, order="F")).cuda()
+    dB = torch.from_numpy(B.reshape(-1, order="F")).cuda()
+    dC = torch.empty(n * n, dtype=torch.float64, device="cuda")
+    info = cg.dgemm_ozaki2_device("N", "N", n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n)
+    dE, dR = torch.empty_like(dC), torch.empty_like(dC)
+    cg.dgemm_ozaki2_residual("N", "N", n, n, n, dA, n, dB, n, dC, n, dE, dR, n, moduli=28)
+    absab = torch.empty_like(dC)
+    cg.dgemm_ozaki2_device("N", "N", n, n, n, 1.0, dA.abs(), n, dB.abs(), n, 0.0, absab, n, moduli=8)
+    torch.cuda.synchronize()
+    assert not torch.isnan(dE).any()
+    nz = dR != 0
+    rel = (dE.abs()[nz] / dR.abs()[nz])
+    normwise = dE.abs() / absab
+    assert float(normwise.max()) <= 2.0 ** -52, info
+    assert float(rel.max()) <= 1e-15, (float(rel.max()), int((rel > 1e-15).sum()), info)
