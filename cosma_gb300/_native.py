@@ -26,7 +26,7 @@ class CosmaGpuError(RuntimeError):
 class OzakiInfo(C.Structure):
     _fields_ = [("slices", C.c_int), ("products", C.c_int), ("groups", C.c_int), ("fallback_native", C.c_int),
                 ("spread_bits", C.c_double), ("prep_ms", C.c_double), ("gemm_ms", C.c_double),
-                ("fraction_bits", C.c_int)]
+                ("fraction_bits", C.c_int), ("exact_product", C.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -106,7 +106,7 @@ SIGNATURES = {
                                             C.POINTER(OzakiInfo)]),
     "cosma_gpu_dgemm_ozaki2_residual": (i32, [ch, ch, i64, i64, i64, vp, i64, vp, i64, vp, i64, i32, vp, vp, i64, vp,
                                               C.POINTER(OzakiInfo)]),
-    "cosma_gpu_ozaki2_choose": (i32, [i64, dbl, i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "cosma_gpu_ozaki2_choose": (i32, [i64, dbl, i32, i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cosma_gpu_dgemm_ozaki_noalloc": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                             C.POINTER(OzakiInfo)]),
     "cosma_gpu_grouped_plan_create": (vp, [i32, i32, C.POINTER(GemmProblem), i32, vp]),

@@ -281,11 +281,12 @@ def dgemm_ozaki2_residual(transa, transb, m, n, k, A, lda, B, ldb, Ct, ldt, E, R
     return info.as_dict()
 
 
-def ozaki2_choose(k, spread_bits=0.0, moduli=0):
+def ozaki2_choose(k, spread_bits=0.0, moduli=0, exact_bits=0):
     """(modulus count, fraction bits P) the Chinese-remainder form uses (host only)."""
     lib = N.load()
     nm, P = C.c_int(), C.c_int()
-    N.check(lib.cosma_gpu_ozaki2_choose(int(k), float(spread_bits), int(moduli), C.byref(nm), C.byref(P)))
+    N.check(lib.cosma_gpu_ozaki2_choose(int(k), float(spread_bits), int(exact_bits), int(moduli), C.byref(nm),
+                                        C.byref(P)))
     return nm.value, P.value
 
 

@@ -30,7 +30,7 @@ void DeviceBuffer::release() {
 static bool is_zero(const double* v, Scalar s) { return v[0] == 0.0 && (!scalar_complex(s) || v[1] == 0.0); }
 
 int gemm_device(const GemmDesc& g, int method, int ozaki_slices, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     if (g.m < 0 || g.n < 0 || g.k < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: negative size");
     if (g.opa < 0 || g.opb < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "gemm: op must be N, T or C");
     if (g.m == 0 || g.n == 0) return COSMA_GPU_SUCCESS;

@@ -20,6 +20,8 @@
 #include "common.cuh"
 #include "runtime.hpp"
 
+#include <cmath>
+
 namespace cgb {
 namespace {
 
@@ -119,14 +121,57 @@ __device__ __forceinline__ R sub_rn(R a, R b);
 template <> __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 template <> __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
-// real: d = fl(fl(alpha*s) + fl(beta*d)); beta == 0 -> d = fl(alpha*s)
+// fl(s * x) for a scale s = 2^e.  A normal x whose scaled exponent stays
+// normal is scaled exactly by moving its exponent field - integer work
+// instead of an FP64 multiply (GB300's FP64 pipe, not HBM, bounds the
+// unpack otherwise); zeros, subnormals, Inf/NaN and results that leave the
+// normal range take the multiply, so the result is fl(s*x) bit for bit.
+__device__ __forceinline__ double mul_pow2(double s, int e, double x) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7FF), ne = ex + e;
+    if (ex == 0 || ex == 0x7FF || ne <= 0 || ne >= 0x7FF) return __dmul_rn(s, x);
+    return __longlong_as_double(b + ((long long)e << 52));
+}
+__device__ __forceinline__ float mul_pow2(float s, int e, float x) {
+    const int b = __float_as_int(x);
+    const int ex = (b >> 23) & 0xFF, ne = ex + e;
+    if (ex == 0 || ex == 0xFF || ne <= 0 || ne >= 0xFF) return __fmul_rn(s, x);
+    return __int_as_float(b + (e << 23));
+}
+
+// How a real scale is applied: 0 = identity (s == 1), 1 = exponent shift
+// (s a power of two, exponent e), 2 = multiply.
 template <class R>
-__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, const R* __restrict__ src, int64_t lds,
-                                   R beta, R* __restrict__ dst, int64_t ldd, int read_dst) {
+struct ScaleMode {
+    int mode, e;
+};
+template <class R>
+__host__ ScaleMode<R> scale_mode(double s) {
+    int e = 0;
+    const double f = std::frexp(s, &e);  // s = f * 2^e, f in [0.5, 1)
+    if (s == 1.0) return {0, 0};
+    if (f == 0.5 && std::isfinite(s)) return {1, e - 1};
+    return {2, 0};
+}
+template <class R>
+__device__ __forceinline__ R apply_scale(const ScaleMode<R>& m, R s, R x) {
+    if (m.mode == 0) return x;
+    if (m.mode == 1) return mul_pow2(s, m.e, x);
+    return mul_rn(s, x);
+}
+
+// real: d = fl(fl(alpha*s) + fl(beta*d)); beta == 0 -> d = fl(alpha*s).  The
+// modes only choose how each (exact or rounded) product is formed, never the
+// result: a multiply by 1 or by a power of two is exact unless it leaves the
+// normal range, where mul_pow2 multiplies.
+template <class R>
+__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, ScaleMode<R> am, const R* __restrict__ src,
+                                   int64_t lds, R beta, ScaleMode<R> bm, R* __restrict__ dst, int64_t ldd,
+                                   int read_dst) {
     for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-            R v = mul_rn(alpha, src[i + j * lds]);
-            if (read_dst) v = add_rn(v, mul_rn(beta, dst[i + j * ldd]));
+            R v = apply_scale(am, alpha, src[i + j * lds]);
+            if (read_dst) v = add_rn(v, apply_scale(bm, beta, dst[i + j * ldd]));
             dst[i + j * ldd] = v;
         }
 }
@@ -176,7 +221,7 @@ __global__ void scale_cplx_kernel(int64_t rows, int64_t cols, R br, R bi, V* C, 
 
 dim3 grid2d(int64_t rows, int64_t cols, int threads) {
     int64_t bx = ceil_div(rows, threads);
-    if (bx > 64) bx = 64;
+    if (bx > 64) bx = 64;  // columns beyond the grid's height are strided; rows beyond 64 blocks too
     int64_t by = cols < 65535 ? cols : 65535;
     if (by < 1) by = 1;
     if (bx < 1) bx = 1;
@@ -239,12 +284,14 @@ int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, co
     dim3 g = grid2d(rows, cols, 256);
     switch (sc) {
         case Scalar::D:
-            unpack_real_kernel<double><<<g, 256, 0, s>>>(rows, cols, alpha[0], (const double*)src, lds, beta[0],
+            unpack_real_kernel<double><<<g, 256, 0, s>>>(rows, cols, alpha[0], scale_mode<double>(alpha[0]),
+                                                         (const double*)src, lds, beta[0], scale_mode<double>(beta[0]),
                                                          (double*)dst, ldd, read_dst);
             break;
         case Scalar::S:
-            unpack_real_kernel<float><<<g, 256, 0, s>>>(rows, cols, (float)alpha[0], (const float*)src, lds,
-                                                        (float)beta[0], (float*)dst, ldd, read_dst);
+            unpack_real_kernel<float><<<g, 256, 0, s>>>(rows, cols, (float)alpha[0], scale_mode<float>((float)alpha[0]),
+                                                        (const float*)src, lds, (float)beta[0],
+                                                        scale_mode<float>((float)beta[0]), (float*)dst, ldd, read_dst);
             break;
         case Scalar::Z:
             unpack_cplx_kernel<double, double2><<<g, 256, 0, s>>>(rows, cols, alpha[0], alpha[1],

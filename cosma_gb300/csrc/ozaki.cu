@@ -87,14 +87,15 @@ __global__ void scale_kcontig_kernel(const double* __restrict__ X, int64_t ld, i
     unsigned bad = 0;
     const double* p = X + row * ld;
     for (int64_t l = lane; l < k; l += 32) {
-        int lb;
-        if (element_log2(p[l], &lb, &bad)) state_add(s, lb);
+        int lb, lsb;
+        if (element_log2(p[l], &lb, &bad, &lsb)) state_add(s, lb, lsb);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         RowState t;
         t.emax = __shfl_xor_sync(0xffffffffu, s.emax, o);
         t.mass = __shfl_xor_sync(0xffffffffu, s.mass, o);
+        t.lsbmin = __shfl_xor_sync(0xffffffffu, s.lsbmin, o);
         s = state_merge(s, t);
     }
     bad = __any_sync(0xffffffffu, bad);
@@ -108,9 +109,11 @@ __global__ void scale_kcontig_kernel(const double* __restrict__ X, int64_t ld, i
 // one thread per row over a chunk of K; partial states combined afterwards.
 // es = 2 for complex data viewed as doubles: element (row, l) is the pair
 // X[2*row + l*ld], X[2*row + 1 + l*ld] and both parts count.
+// pl (nullable) receives each chunk's lowest set-bit weight, for callers
+// that need the fraction bits keeping every element exact.
 __global__ void scale_mcontig_partial_kernel(const double* __restrict__ X, int64_t ld, int es, int64_t rows,
                                              int64_t k, int64_t kchunk, int* __restrict__ pe,
-                                             float* __restrict__ pm, Stats* st) {
+                                             float* __restrict__ pm, int* __restrict__ pl, Stats* st) {
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     const int64_t l0 = (int64_t)blockIdx.y * kchunk, l1 = min(k, l0 + kchunk);
@@ -118,22 +121,24 @@ __global__ void scale_mcontig_partial_kernel(const double* __restrict__ X, int64
     unsigned bad = 0;
     for (int64_t l = l0; l < l1; ++l) {
         for (int c = 0; c < es; ++c) {
-            int lb;
-            if (element_log2(X[row * es + c + l * ld], &lb, &bad)) state_add(s, lb);
+            int lb, lsb;
+            if (element_log2(X[row * es + c + l * ld], &lb, &bad, &lsb)) state_add(s, lb, lsb);
         }
     }
     if (bad) atomicOr(&st->nonfinite, 1u);
     pe[blockIdx.y * rows + row] = s.emax;
     pm[blockIdx.y * rows + row] = s.mass;
+    if (pl) pl[blockIdx.y * rows + row] = s.lsbmin;
 }
 
-__global__ void scale_mcontig_combine_kernel(const int* __restrict__ pe, const float* __restrict__ pm, int nchunks,
-                                             int64_t rows, int64_t k, int* __restrict__ exp_out, Stats* st,
-                                             int which) {
+__global__ void scale_mcontig_combine_kernel(const int* __restrict__ pe, const float* __restrict__ pm,
+                                             const int* __restrict__ pl, int nchunks, int64_t rows, int64_t k,
+                                             int* __restrict__ exp_out, Stats* st, int which) {
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     RowState s{-(1 << 30), 0.0f};
-    for (int c = 0; c < nchunks; ++c) s = state_merge(s, RowState{pe[c * rows + row], pm[c * rows + row]});
+    for (int c = 0; c < nchunks; ++c)
+        s = state_merge(s, RowState{pe[c * rows + row], pm[c * rows + row], pl ? pl[c * rows + row] : (1 << 30)});
     finish_row(s, k, exp_out + row, st, which);
 }
 
@@ -632,12 +637,13 @@ int scale_operand(bool kcontig, const double* X, int64_t ld, int64_t rows, int64
         int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
         nchunks = (int)std::min<int64_t>(nchunks, std::max<int64_t>(1, k / 64));
         const int64_t kchunk = ceil_div(k, nchunks);
-        CGB_CHECK(part.reserve((size_t)nchunks * rows * 8, st));
+        CGB_CHECK(part.reserve((size_t)nchunks * rows * 12, st));
         int* pe = (int*)part.ptr;
         float* pm = (float*)((char*)part.ptr + (size_t)nchunks * rows * 4);
+        int* pl = (int*)((char*)part.ptr + (size_t)nchunks * rows * 8);
         scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
-            X, ld * es, es, rows, k, kchunk, pe, pm, st_dev);
-        scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, rows, k * es, exps,
+            X, ld * es, es, rows, k, kchunk, pe, pm, pl, st_dev);
+        scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, pl, nchunks, rows, k * es, exps,
                                                                             st_dev, which);
     }
     CGB_CUDA(cudaGetLastError());
@@ -998,7 +1004,7 @@ int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: buffers must be 8-byte aligned");
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: m and n are limited to 2^24");
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     // K beyond one exact accumulator pass is cut into chunks accumulated
     // through C (beta = 1 after the first chunk).
     GemmDesc c = g;
@@ -1019,7 +1025,7 @@ int ozaki_zgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_oz
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: complex buffers must be 16-byte aligned");
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 23)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: m is limited to 2^24 and n to 2^23 (complex)");
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     // each complex term is two real terms: half the real pass length per chunk
     const int64_t kmax = oz::MAX_K_PER_CALL / 2;
     GemmDesc c = g;
@@ -1161,9 +1167,9 @@ int noalloc_chunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozak
             int* pe = (int*)part;
             float* pm = (float*)(part + (size_t)nchunks * o.rows * 4);
             scale_mcontig_partial_kernel<<<dim3((unsigned)row_blocks, (unsigned)nchunks), 256, 0, st>>>(
-                o.X, o.ld, 1, o.rows, k, kchunk, pe, pm, st_dev);
-            scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nchunks, o.rows, k, o.exps,
-                                                                                st_dev, o.which);
+                o.X, o.ld, 1, o.rows, k, kchunk, pe, pm, nullptr, st_dev);
+            scale_mcontig_combine_kernel<<<(unsigned)row_blocks, 256, 0, st>>>(pe, pm, nullptr, nchunks, o.rows, k,
+                                                                                o.exps, st_dev, o.which);
         }
         CGB_CUDA(cudaGetLastError());
     }
@@ -1237,7 +1243,7 @@ extern "C" int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m
                                              cosma_gpu_ozaki_info* info) {
     using namespace cgb;
     clear_error();
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     const int opa = parse_op(transa), opb = parse_op(transb);
     if (opa < 0 || opb < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: op must be N, T or C");
     if (m < 0 || n < 0 || k < 0) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki no-alloc: negative size");

@@ -89,28 +89,29 @@ __device__ __forceinline__ uint32_t mod32(uint32_t u, uint32_t p, uint32_t magic
     return r >= p ? r - p : r;
 }
 
-constexpr int LIMB18 = 7;  // 18-bit limbs of a scaled integer (P <= 120: at most 121 bits)
+constexpr int LIMB13 = 9;  // 13-bit limbs of a scaled integer (P <= 116: at most 117 bits)
 
 struct SplitParams {
     int nmod;
     int P;      // fraction bits
-    int limbs;  // 18-bit limbs the scaled integers need: ceil((P + 1) / 18)
-    uint32_t p[MAX_MODULI], magic[MAX_MODULI];
-    uint32_t c18[MAX_MODULI][LIMB18];  // 2^(18 i) mod p
+    int limbs;  // 13-bit limbs the scaled integers need: ceil((P + 1) / 13)
+    uint32_t p[MAX_MODULI], magic[MAX_MODULI], h[MAX_MODULI];  // magic = ceil(2^32 / p), h = floor(p / 2)
+    float bias[MAX_MODULI];                                      // -(2^23 + h)
+    uint32_t c13[MAX_MODULI][LIMB13];                            // 2^(13 i) mod p
 };
 
 // The scaled integer X = round_half_away(|x| 2^(P - E)) of one operand
-// element as 18-bit limbs (X < 2^(P+1)), with its sign.  |x| = M 2^eu with
-// the 53-bit significand M; X = M 2^sh exactly when sh >= 0.
+// element as 13-bit limbs (X < 2^(P+1)), with its sign as +-1.0f.  |x| = M
+// 2^eu with the 53-bit significand M; X = M 2^sh exactly when sh >= 0.
 struct Scaled {
-    uint32_t d[LIMB18];
-    bool neg;
+    uint32_t d[LIMB13];
+    float sgn;
 };
 
 __device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     Scaled v;
-    v.neg = (b >> 63) != 0;
+    v.sgn = (b >> 63) ? -1.0f : 1.0f;
     const int ef = (int)((b >> 52) & 0x7FF);
     unsigned long long M = b & 0xFFFFFFFFFFFFFull;
     int eu;
@@ -122,39 +123,44 @@ __device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
         M = r > 63 ? 0ull : (M + (1ull << (r - 1))) >> r;
         sh = 0;
     }
-    // X = M << sh as a 128-bit integer (hi:lo), then cut into 18-bit limbs
+    // X = M << sh as a 128-bit integer (hi:lo), then cut into 13-bit limbs
     unsigned long long lo, hi;
     if (sh == 0) { lo = M; hi = 0; }
     else if (sh < 64) { lo = M << sh; hi = M >> (64 - sh); }
     else { lo = 0; hi = M << (sh - 64); }
 #pragma unroll
-    for (int i = 0; i < LIMB18; ++i) {
-        const int pos = 18 * i;
+    for (int i = 0; i < LIMB13; ++i) {
+        const int pos = 13 * i;
         unsigned long long w;
-        if (pos + 18 <= 64) w = lo >> pos;
+        if (pos + 13 <= 64) w = lo >> pos;
         else if (pos >= 64) w = hi >> (pos - 64);
         else w = (lo >> pos) | (hi << (64 - pos));
-        v.d[i] = (uint32_t)w & 0x3FFFFu;
+        v.d[i] = (uint32_t)w & 0x1FFFu;
     }
     return v;
 }
 
-// Balanced residue of X modulo p, sign applied: sum_i d_i (2^(18 i) mod p) is
-// below 7 * 2^18 * 2^8 < 2^29, so one reduction finishes it.  The result lies
-// in [-(p-1)/2, p/2] ([-126, 127] for p = 254) before the sign.
+// FP32 bits of the balanced residue of the signed scaled integer modulo p,
+// b = ((X + h) mod p) - h in [-h, p - 1 - h] (|b| <= 127), sign applied.
+// u = X_0 + h + sum_i X_i (2^(13 i) mod p) stays below 2^24 (NL <= 9), where
+// umulhi(u, ceil(2^32 / p)) is exactly floor(u / p) for every modulus here
+// (checked exhaustively), so r = u - q p needs no correction.  The value is
+// then formed on the FP32 pipe: 2^23 + r has the bits 0x4B000000 | r, and
+// (2^23 + r - 2^23 - h) * sign is exact.  Its upper 16 bits are its BF16
+// encoding (exact: at most 8 significant bits).
 template <int NL>
-__device__ __forceinline__ int balanced_residue(const Scaled& v, uint32_t p, uint32_t magic, const uint32_t* c18) {
-    uint32_t u = v.d[0];
+__device__ __forceinline__ uint32_t residue_bits(const Scaled& v, uint32_t p, uint32_t magic, uint32_t h, float bias,
+                                                 const uint32_t* c13) {
+    uint32_t u = v.d[0] + h;
 #pragma unroll
-    for (int i = 1; i < NL; ++i) u += v.d[i] * c18[i];
-    int s = (int)mod32(u, p, magic);
-    if (s > (int)(p >> 1)) s -= (int)p;
-    return v.neg ? -s : s;
+    for (int i = 1; i < NL; ++i) u += v.d[i] * c13[i];
+    const uint32_t r = u - __umulhi(u, magic) * p;
+    const float f = (__uint_as_float(0x4B000000u | r) + bias) * v.sgn;
+    return __float_as_uint(f);
 }
 
-// BF16 bits of a small integer (|v| <= 256): the upper half of its FP32 bits,
-// exact because the value needs at most 8 significant bits.
-__device__ __forceinline__ uint32_t bf16_bits(int v) { return __float_as_uint((float)v) >> 16; }
+// Two FP32 residues packed as two BF16 values (upper halves), low one first.
+__device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) { return __byte_perm(lo, hi, 0x7632); }
 
 // Residue matrices of a real (rows x k) operand: N BF16 matrices [t][rows_pad][k_pad],
 // zero padded.  A block of 256 threads covers 32 rows x 64 K elements, each
@@ -166,12 +172,11 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
                                                     int64_t k, const int* __restrict__ exps, int64_t k_pad,
                                                     int64_t rows_pad, uint16_t* __restrict__ out,
                                                     const __grid_constant__ SplitParams sp) {
+    // a warp covers 4 rows x 64 K elements: its stores are four 128-byte row
+    // segments per modulus, its loads (either layout) whole 32-byte sectors
     const int t = threadIdx.x;
-    int64_t r;
-    int kc;
-    if (KCONTIG) { r = (int64_t)blockIdx.x * 32 + t / 8; kc = t % 8; }
-    else { r = (int64_t)blockIdx.x * 32 + t % 32; kc = t / 32; }
-    const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 8;
+    const int64_t r = (int64_t)blockIdx.x * 32 + t / 8;
+    const int64_t l0 = (int64_t)blockIdx.y * 64 + (t % 8) * 8;
     if (r >= rows_pad || l0 >= k_pad) return;
     const int E = r < rows ? exps[r] : 0;
     Scaled v[8];
@@ -186,14 +191,13 @@ __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X
     const int64_t slab = rows_pad * k_pad;
 #pragma unroll 1
     for (int m = 0; m < sp.nmod; ++m) {
-        const uint32_t p = sp.p[m], mg = sp.magic[m];
+        const uint32_t p = sp.p[m], mg = sp.magic[m], h = sp.h[m];
+        const float bias = sp.bias[m];
         uint32_t w[4];
 #pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-            const uint32_t lo = bf16_bits(balanced_residue<NL>(v[e], p, mg, sp.c18[m]));
-            const uint32_t hi = bf16_bits(balanced_residue<NL>(v[e + 1], p, mg, sp.c18[m]));
-            w[e / 2] = lo | (hi << 16);
-        }
+        for (int e = 0; e < 8; e += 2)
+            w[e / 2] = pack_bf16(residue_bits<NL>(v[e], p, mg, h, bias, sp.c13[m]),
+                                 residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m]));
         *reinterpret_cast<uint4*>(o + m * slab) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
@@ -213,12 +217,9 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
                                                          int64_t rows_pad, int64_t slice_rows, int conj,
                                                          uint16_t* __restrict__ out,
                                                          const __grid_constant__ SplitParams sp) {
-    const int t = threadIdx.x;
-    int64_t r;
-    int kc;
-    if (KCONTIG) { r = (int64_t)blockIdx.x * 32 + t / 8; kc = t % 8; }
-    else { r = (int64_t)blockIdx.x * 32 + t % 32; kc = t / 32; }
-    const int64_t l0 = (int64_t)blockIdx.y * 64 + kc * 8;
+    const int t = threadIdx.x;  // a warp covers 4 rows x 64 K elements (see split_kernel)
+    const int64_t r = (int64_t)blockIdx.x * 32 + t / 8;
+    const int64_t l0 = (int64_t)blockIdx.y * 64 + (t % 8) * 8;
     if (r >= rows_pad || l0 >= kh) return;
     const int E = r < rows ? exps[r] : 0;
     const int64_t pitch = 2 * kh, slab = slice_rows * pitch;
@@ -232,18 +233,18 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
             double x = 0.0;
             if (r < rows && l < k) x = Xd[2 * (KCONTIG ? l + r * ld : r + l * ld) + part];
             v[e] = scaled_integer(x, E, sp.P);
-            if (part && conj) v[e].neg = !v[e].neg;  // the conjugated imaginary part
+            if (part && conj) v[e].sgn = -v[e].sgn;  // the conjugated imaginary part
         }
 #pragma unroll 1
         for (int m = 0; m < sp.nmod; ++m) {
-            const uint32_t p = sp.p[m], mg = sp.magic[m];
+            const uint32_t p = sp.p[m], mg = sp.magic[m], h = sp.h[m];
+            const float bias = sp.bias[m];
             uint32_t w[4], nw[4];
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
-                const int a = balanced_residue<NL>(v[e], p, mg, sp.c18[m]);
-                const int b = balanced_residue<NL>(v[e + 1], p, mg, sp.c18[m]);
-                w[e / 2] = bf16_bits(a) | (bf16_bits(b) << 16);
-                nw[e / 2] = bf16_bits(-a) | (bf16_bits(-b) << 16);
+                w[e / 2] = pack_bf16(residue_bits<NL>(v[e], p, mg, h, bias, sp.c13[m]),
+                                     residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m]));
+                nw[e / 2] = w[e / 2] ^ 0x80008000u;  // the negated pair: both sign bits flipped
             }
             uint16_t* base = out + m * slab;
             const uint4 val = make_uint4(w[0], w[1], w[2], w[3]);
@@ -460,10 +461,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 // ------------------------------------------------------------- reconstruction
 struct CombineParams {
     int nmod, twoP;
-    int shift;        // bit offset of the quotient estimate (bit length of M minus 24)
-    float inv_mhi;    // 1 / (M >> shift)
     uint32_t w[MAX_MODULI][LIMBS];  // CRT weights w_t = (M/p_t) * ((M/p_t)^-1 mod p_t)
-    uint32_t M[LIMBS], halfM[LIMBS];
+    uint32_t M[LIMBS];
+    float inv_m2;                   // 2^(32 (L-2)) / M for the quotient estimate (L: the kernel's limbs)
     int64_t m, n, ldc, m_pad, nb16, row_blocks;
     int64_t n_split;  // complex: GEMM columns [0, n_split) are real parts, the rest imaginary parts
     int cs;           // doubles per element of C (1 real, 2 complex)
@@ -480,80 +480,78 @@ struct CombineParams {
     double* Rx;
 };
 
-// Bits [s, s + 64) of the L-limb integer x (static limb indices only).
-template <int L>
-__device__ __forceinline__ unsigned long long bits64(const uint32_t (&x)[L], int s) {
-    unsigned long long v = 0;
-#pragma unroll
-    for (int l = 0; l < L; ++l) {
-        const int pos = 32 * l - s;  // where bit 0 of limb l lands
-        if (pos >= 64 || pos <= -32) continue;
-        const unsigned long long limb = x[l];
-        v |= pos >= 0 ? (limb << pos) : (limb >> -pos);
+// Round-to-nearest-even conversion of the unsigned 128-bit integer (hi:lo)
+// times 2^e2 to double (subnormal and overflow results included).
+__device__ __forceinline__ double u128_to_double(unsigned long long lo, unsigned long long hi, int e2) {
+    if (hi == 0 && lo == 0) return 0.0;
+    const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+    int e_lsb = msb - 52 + e2;  // weight of the last kept bit for a normal result
+    int r = msb - 52;           // bits dropped
+    if (e_lsb < -1074) {        // subnormal result: fixed last-bit weight 2^-1074
+        r += -1074 - e_lsb;
+        e_lsb = -1074;
     }
-    return v;
+    unsigned long long mant;
+    if (r <= 0) {
+        mant = lo << (-r);  // msb <= 52: the value fits in lo
+    } else if (r > 127) {
+        mant = 0;  // far below the smallest subnormal
+    } else {
+        unsigned long long q, g, st;  // kept bits, guard bit, sticky bits
+        if (r < 64) {
+            q = (lo >> r) | (hi << (64 - r));
+            g = (lo >> (r - 1)) & 1ull;
+            st = (r - 1) > 0 ? (lo & ((1ull << (r - 1)) - 1ull)) : 0ull;
+        } else if (r == 64) {
+            q = hi;
+            g = lo >> 63;
+            st = lo & 0x7FFFFFFFFFFFFFFFull;
+        } else {
+            q = hi >> (r - 64);
+            g = (hi >> (r - 65)) & 1ull;
+            st = lo | ((r - 65) > 0 ? (hi & ((1ull << (r - 65)) - 1ull)) : 0ull);
+        }
+        mant = q;
+        if (g && (st || (mant & 1ull))) ++mant;
+    }
+    const bool normal = e_lsb > -1074 || mant >= (1ull << 52);
+    if (mant >= (1ull << 53)) {  // rounding carried into a new bit
+        mant >>= 1;
+        ++e_lsb;
+    }
+    unsigned long long bits;
+    if (normal && mant >= (1ull << 52)) {
+        const int be = e_lsb + 52 + 1023;
+        bits = be >= 2047 ? 0x7FF0000000000000ull : (((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull));
+    } else {
+        bits = mant;  // subnormal (or the smallest normal reached by rounding)
+    }
+    return __longlong_as_double((long long)bits);
 }
 
-// Whether any bit below bit s of x is set.
-template <int L>
-__device__ __forceinline__ bool any_below(const uint32_t (&x)[L], int s) {
-    uint32_t any = 0;
-#pragma unroll
-    for (int l = 0; l < L; ++l) {
-        const int lo = 32 * l;
-        if (lo + 32 <= s) any |= x[l];
-        else if (lo < s) any |= x[l] & ((1u << (s - lo)) - 1u);
-    }
-    return any != 0;
-}
-
-// x -= y (returns the borrow out).
-template <int L>
-__device__ __forceinline__ uint32_t sub_limbs(uint32_t (&x)[L], const uint32_t* y) {
-    unsigned long long br = 0;
-#pragma unroll
-    for (int l = 0; l < L; ++l) {
-        const unsigned long long d = (unsigned long long)x[l] - y[l] - br;
-        x[l] = (uint32_t)d;
-        br = (d >> 63) & 1ull;
-    }
-    return (uint32_t)br;
-}
-template <int L>
-__device__ __forceinline__ void add_limbs(uint32_t (&x)[L], const uint32_t* y) {
-    unsigned long long c = 0;
-#pragma unroll
-    for (int l = 0; l < L; ++l) {
-        c += (unsigned long long)x[l] + y[l];
-        x[l] = (uint32_t)c;
-        c >>= 32;
-    }
-}
-// Sign of x - y: the highest differing limb decides.
-template <int L>
-__device__ __forceinline__ int cmp_limbs(const uint32_t (&x)[L], const uint32_t* y) {
-    int c = 0;
-#pragma unroll
-    for (int l = 0; l < L; ++l)
-        if (x[l] != y[l]) c = x[l] > y[l] ? 1 : -1;
-    return c;
-}
-
-// |x| * 2^e2 rounded once to FP64 (round to nearest even), negated if neg:
-// the top 127 bits with the bits below folded into a sticky last bit (below
-// the rounding position whenever bits were dropped, so the rounding is
-// unaffected); bit 127 of the window stays clear, it is the converter's sign.
+// |x| (L limbs) * 2^e2 rounded once to FP64, negated if neg: the top four
+// limbs from the highest nonzero one, the limbs below folded into a sticky
+// last bit (below the rounding position: the window keeps 97+ bits).
 template <int L>
 __device__ __forceinline__ double limbs_to_double(const uint32_t (&x)[L], bool neg, int e2) {
-    int top = -1;
+    int tl = -1;
 #pragma unroll
     for (int l = 0; l < L; ++l)
-        if (x[l]) top = 32 * l + 31 - __clz((int)x[l]);
-    if (top < 0) return 0.0;
-    const int b0 = top > 126 ? top - 126 : 0;
-    unsigned long long lo = bits64<L>(x, b0), hi = bits64<L>(x, b0 + 64);
-    if (b0 > 0 && any_below<L>(x, b0)) lo |= 1ull;
-    const double r = oz::i128_to_double(lo, hi, e2 + b0);
+        if (x[l]) tl = l;
+    if (tl < 0) return 0.0;
+    uint32_t w3 = 0, w2 = 0, w1 = 0, w0 = 0, sticky = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        const uint32_t v = x[l];
+        if (l == tl) w3 = v;
+        else if (l == tl - 1) w2 = v;
+        else if (l == tl - 2) w1 = v;
+        else if (l == tl - 3) w0 = v;
+        else if (l < tl - 3) sticky |= v;
+    }
+    const unsigned long long hi = ((unsigned long long)w3 << 32) | w2;
+    const unsigned long long lo = ((unsigned long long)w1 << 32) | w0 | (sticky ? 1ull : 0ull);
+    const double r = u128_to_double(lo, hi, e2 + 32 * (tl - 3));
     return neg ? -r : r;
 }
 
@@ -570,36 +568,37 @@ __device__ __forceinline__ void set_shifted(uint32_t (&x)[L], unsigned long long
     }
 }
 
-// One output element per thread: a block of 16 warps covers 32 rows x 16
-// GEMM columns (block b: row block b % row_blocks, column block b /
-// row_blocks); warp w takes column 16*cb + w, lane the row 32*rb + lane, so
-// that the 16 warps read the 512 contiguous residue bytes of each modulus
-// together.
-template <int L, bool RESIDUAL>
-__global__ void __launch_bounds__(512) combine_kernel(const __grid_constant__ CombineParams p) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t rb = (int64_t)blockIdx.x % p.row_blocks, cb = (int64_t)blockIdx.x / p.row_blocks;
-    const int64_t i = rb * 32 + lane;
-    const int64_t gj = cb * 16 + w;  // GEMM column
-    int64_t j = gj;
-    int part = 0;
-    if (j >= p.n_split) {
-        j -= p.n_split;
-        part = 1;
-    }
-    if (i >= p.m || j >= p.n) return;
-    const uint8_t* rp = p.R + (cb * p.m_pad + i) * 16 + w;
-    const int64_t stride = p.nb16 * p.m_pad * 16;
-    unsigned long long acc[L];
+template <int L>
+__device__ __forceinline__ void negate_limbs(uint32_t (&x)[L]) {
+    unsigned long long c = 1;
 #pragma unroll
-    for (int l = 0; l < L; ++l) acc[l] = 0;
-#pragma unroll 4
-    for (int t = 0; t < p.nmod; ++t) {
-        const uint32_t r = rp[t * stride];
-#pragma unroll
-        for (int l = 0; l < L; ++l) acc[l] += (unsigned long long)r * p.w[t][l];
+    for (int l = 0; l < L; ++l) {
+        c += (uint32_t)~x[l];
+        x[l] = (uint32_t)c;
+        c >>= 32;
     }
-    uint32_t x[L];
+}
+
+// x -= y (two's complement over L limbs).
+template <int L>
+__device__ __forceinline__ void sub_limbs(uint32_t (&x)[L], const uint32_t (&y)[L]) {
+    unsigned long long br = 0;
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+        const unsigned long long d = (unsigned long long)x[l] - y[l] - br;
+        x[l] = (uint32_t)d;
+        br = (d >> 63) & 1ull;
+    }
+}
+
+// V from X = sum_t r_t w_t (L 64-bit partial limbs): carries, then one
+// subtraction of q M with q = rint(X / M) estimated in FP32 from the top three
+// limbs (error < 0.003).  |V| <= M/4 (the modulus count is chosen so), so
+// X - q M lies in (-0.51 M, 0.51 M) and is V itself, as an L-limb two's
+// complement number.  Returns |V| in x and its sign.
+template <int L>
+__device__ __forceinline__ bool reduce_crt(const unsigned long long (&acc)[L], uint32_t (&x)[L],
+                                           const CombineParams& p) {
     unsigned long long c = 0;
 #pragma unroll
     for (int l = 0; l < L; ++l) {
@@ -607,78 +606,102 @@ __global__ void __launch_bounds__(512) combine_kernel(const __grid_constant__ Co
         x[l] = (uint32_t)c;
         c >>= 32;
     }
-    // x mod M: the quotient estimate is floor(x/M) or off by one either way
-    const unsigned long long xh = bits64<L>(x, p.shift);
-    const uint32_t q = (uint32_t)((float)xh * p.inv_mhi);
-    if (q) {
-        unsigned long long br = 0, cm = 0;
+    const float xs = __uint2float_rn(x[L - 1]) * 4294967296.0f + __uint2float_rn(x[L - 2]) +
+                     __uint2float_rn(x[L - 3]) * 2.3283064365386963e-10f;
+    const uint32_t q = __float2uint_rn(xs * p.inv_m2);
+    unsigned long long br = 0, cm = 0;
 #pragma unroll
-        for (int l = 0; l < L; ++l) {  // x -= q * M
-            cm += (unsigned long long)q * p.M[l];
-            const unsigned long long d = (unsigned long long)x[l] - (uint32_t)cm - br;
-            x[l] = (uint32_t)d;
-            br = (d >> 63) & 1ull;
-            cm >>= 32;
+    for (int l = 0; l < L; ++l) {  // x -= q * M
+        cm += (unsigned long long)q * p.M[l];
+        const unsigned long long d = (unsigned long long)x[l] - (uint32_t)cm - br;
+        x[l] = (uint32_t)d;
+        br = (d >> 63) & 1ull;
+        cm >>= 32;
+    }
+    const bool neg = (x[L - 1] >> 31) != 0;
+    if (neg) negate_limbs<L>(x);
+    return neg;
+}
+
+// Four output elements per thread: a block of 4 warps covers 32 rows x 16
+// GEMM columns (block b: row block b % row_blocks, column block b /
+// row_blocks); warp g takes columns 16 cb + 4 g .. + 3, lane the row 32 rb +
+// lane, and one 32-bit load gives the thread its four residues of a modulus.
+template <int L, bool RESIDUAL>
+__global__ void __launch_bounds__(128) combine_kernel(const __grid_constant__ CombineParams p) {
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int64_t rb = (int64_t)blockIdx.x % p.row_blocks, cb = (int64_t)blockIdx.x / p.row_blocks;
+    const int64_t i = rb * 32 + lane;
+    if (i >= p.m) return;
+    const int64_t gj0 = cb * 16 + 4 * g;  // first GEMM column of this thread
+    int64_t j0 = gj0;
+    int part = 0;
+    if (j0 >= p.n_split) {
+        j0 -= p.n_split;
+        part = 1;
+    }
+    if (j0 >= p.n) return;
+    const uint32_t* rp = reinterpret_cast<const uint32_t*>(p.R + (cb * p.m_pad + i) * 16) + g;
+    const int64_t stride = p.nb16 * p.m_pad * 4;  // 32-bit words per modulus
+    unsigned long long acc[4][L];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int l = 0; l < L; ++l) acc[c][l] = 0;
+#pragma unroll 2
+    for (int t = 0; t < p.nmod; ++t) {
+        const uint32_t r4 = __ldg(rp + t * stride);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const uint32_t r = (r4 >> (8 * c)) & 0xFFu;
+#pragma unroll
+            for (int l = 0; l < L; ++l) acc[c][l] += (unsigned long long)r * p.w[t][l];
         }
-        if (br) add_limbs<L>(x, p.M);  // the estimate was one too large
     }
-    if (cmp_limbs<L>(x, p.M) >= 0) sub_limbs<L>(x, p.M);
-    // centre: values above M/2 stand for x - M
-    const bool neg = cmp_limbs<L>(x, p.halfM) > 0;
-    if (neg) {
-        uint32_t y[L];
+    const int Ei = p.expA[i];
 #pragma unroll
-        for (int l = 0; l < L; ++l) y[l] = p.M[l];
-        sub_limbs<L>(y, x);
-#pragma unroll
-        for (int l = 0; l < L; ++l) x[l] = y[l];
-    }
-    // V * 2^(E_i + F_j - 2P), rounded once
-    const int e2 = p.expA[i] + p.expB[j] - p.twoP;
-    double r = limbs_to_double<L>(x, neg, e2);
-    if constexpr (RESIDUAL) {
-        // T = Ct * 2^-e2 is an integer whenever Ct's last bit weighs at least
-        // 2^e2 (always, but for a Ct below ~2^(e2 + 52)); then E = (V - T)
-        // 2^e2 is exact before its one rounding.  Otherwise E is NaN.
-        const double ct = p.Ct[i + j * p.ldt];
-        const unsigned long long b = (unsigned long long)__double_as_longlong(ct);
-        const bool cneg = (b >> 63) != 0;
-        const int ef = (int)((b >> 52) & 0x7FF);
-        unsigned long long mc = b & 0xFFFFFFFFFFFFFull;
-        int ec;
-        if (ef == 0) ec = -1074; else { mc |= 1ull << 52; ec = ef - 1075; }
-        const int s = ec - e2;
-        double err;
-        if (ef == 0x7FF || (mc && (s < 0 || s + 53 > 32 * L - 1))) {
-            err = __longlong_as_double(0x7FF8000000000000ll);
-        } else {
-            uint32_t t[L];
-            set_shifted<L>(t, mc, mc ? s : 0);
-            bool dneg;
-            if (neg == cneg) {  // |V - T| = ||V| - |T||
-                if (cmp_limbs<L>(x, t) >= 0) {
-                    sub_limbs<L>(x, t);
-                    dneg = neg;
-                } else {
-                    sub_limbs<L>(t, x);
-#pragma unroll
-                    for (int l = 0; l < L; ++l) x[l] = t[l];
-                    dneg = !neg;
-                }
-            } else {  // |V - T| = |V| + |T|
-                add_limbs<L>(x, t);
-                dneg = neg;
+    for (int c = 0; c < 4; ++c) {
+        const int64_t j = j0 + c;
+        if (j >= p.n) break;
+        uint32_t x[L];
+        const bool neg = reduce_crt<L>(acc[c], x, p);
+        const int e2 = Ei + p.expB[j] - p.twoP;
+        double r = limbs_to_double<L>(x, neg, e2);
+        if constexpr (RESIDUAL) {
+            // T = Ct * 2^-e2 is an integer whenever Ct's last bit weighs at
+            // least 2^e2 (always, but for a Ct below ~2^(e2 + 52)); then
+            // E = (V - T) 2^e2 is exact before its one rounding.  Otherwise,
+            // or when T does not fit the limbs, E is NaN.
+            const double ct = p.Ct[i + j * p.ldt];
+            const unsigned long long b = (unsigned long long)__double_as_longlong(ct);
+            const bool cneg = (b >> 63) != 0;
+            const int ef = (int)((b >> 52) & 0x7FF);
+            unsigned long long mc = b & 0xFFFFFFFFFFFFFull;
+            int ec;
+            if (ef == 0) ec = -1074; else { mc |= 1ull << 52; ec = ef - 1075; }
+            const int s = ec - e2;
+            double err;
+            if (ef == 0x7FF || (mc && (s < 0 || s + 53 > 32 * L - 2))) {
+                err = __longlong_as_double(0x7FF8000000000000ll);
+            } else {
+                uint32_t t[L];
+                set_shifted<L>(t, mc, mc ? s : 0);
+                if (neg) negate_limbs<L>(x);   // signed V
+                if (cneg) negate_limbs<L>(t);  // signed T
+                sub_limbs<L>(x, t);            // D = V - T, |D| < 2^(32 L - 1)
+                const bool dneg = (x[L - 1] >> 31) != 0;
+                if (dneg) negate_limbs<L>(x);
+                err = limbs_to_double<L>(x, dneg, e2);
             }
-            err = limbs_to_double<L>(x, dneg, e2);
+            p.E[i + j * p.ldo] = err;
+            p.Rx[i + j * p.ldo] = r;
+            continue;
         }
-        p.E[i + j * p.ldo] = err;
-        p.Rx[i + j * p.ldo] = r;
-        return;
+        double* cp = p.C + (i + j * p.ldc) * p.cs + part;
+        if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
+        if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+        *cp = r;
     }
-    double* cp = p.C + (i + j * p.ldc) * p.cs + part;
-    if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
-    if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
-    *cp = r;
 }
 
 // ---------------------------------------------------------------- host side
@@ -701,16 +724,6 @@ struct Big {  // little-endian 32-bit limbs
         for (int i = LIMBS - 1; i >= 0; --i)
             if (w[i]) return 32 * i + 32 - __builtin_clz(w[i]);
         return 0;
-    }
-    unsigned long long bits64(int s) const {
-        unsigned long long v = 0;
-        for (int l = 0; l < LIMBS; ++l) {
-            const int pos = 32 * l - s;
-            if (pos >= 64 || pos <= -32) continue;
-            const unsigned long long limb = w[l];
-            v |= pos >= 0 ? (limb << pos) : (limb >> -pos);
-        }
-        return v;
     }
 };
 
@@ -751,21 +764,23 @@ int requested_fraction_bits(double spread, int64_t k) {
 }
 
 // Modulus count and fraction bits: the caller's count, or the fewest moduli
-// whose product admits the requested fraction bits; P is then the largest
-// the count allows.
-int choose(int nmod_req, double spread, int64_t k, int* nmod, int* P) {
+// that either keep every input bit (exact_bits: then the product is exact
+// and C is correctly rounded) or admit the fraction bits the accuracy rule
+// asks for, whichever is fewer; P is then the largest the count allows.
+int fewest_moduli(int want, int64_t k) {
+    for (int t = 2; t <= MAX_MODULI; ++t)
+        if (max_fraction_bits(t, k) >= want) return t;
+    return MAX_MODULI + 1;
+}
+
+int choose(int nmod_req, double spread, int64_t k, int* nmod, int* P, int exact_bits = 1 << 30) {
     if (nmod_req > 0) {
         *nmod = std::min(nmod_req, MAX_MODULI);
     } else {
-        const int want = requested_fraction_bits(spread, k);
-        *nmod = MAX_MODULI;
-        for (int t = 2; t <= MAX_MODULI; ++t)
-            if (max_fraction_bits(t, k) >= want) {
-                *nmod = t;
-                break;
-            }
+        *nmod = std::min({fewest_moduli(requested_fraction_bits(spread, k), k),
+                          fewest_moduli(std::max(exact_bits, 1), k), MAX_MODULI});
     }
-    *P = std::min(max_fraction_bits(*nmod, k), 120);  // shifts of the split stay below 128
+    *P = std::min(max_fraction_bits(*nmod, k), 116);  // at most nine 13-bit limbs per scaled integer
     if (*P < 1) return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2: too few moduli for this k");
     return COSMA_GPU_SUCCESS;
 }
@@ -774,18 +789,23 @@ void fill_split(SplitParams& sp, int nmod, int P) {
     std::memset(&sp, 0, sizeof(sp));
     sp.nmod = nmod;
     sp.P = P;
-    sp.limbs = (P + 1 + 17) / 18;
+    sp.limbs = (P + 1 + 12) / 13;
     for (int t = 0; t < nmod; ++t) {
         const uint32_t p = kModuli[t];
         sp.p[t] = p;
-        sp.magic[t] = (uint32_t)((1ull << 32) / p);
+        sp.magic[t] = (uint32_t)(((1ull << 32) + p - 1) / p);
+        sp.h[t] = p / 2;
+        sp.bias[t] = -(8388608.0f + (float)(p / 2));
         unsigned long long c = 1;
-        for (int i = 0; i < LIMB18; ++i) {
-            sp.c18[t][i] = (uint32_t)c;
-            c = (c << 18) % p;
+        for (int i = 0; i < LIMB13; ++i) {
+            sp.c13[t][i] = (uint32_t)c;
+            c = (c << 13) % p;
         }
     }
 }
+
+// Limbs the reconstruction needs: sum_t r_t w_t < nmod * 255 * M < 2^(bitlen(M) + 13).
+int limbs_for(int nmod) { return std::max(4, (modulus_product(nmod).bitlen() + 13 + 31) / 32); }
 
 void fill_combine(CombineParams& cp, int nmod, int P) {
     std::memset(&cp, 0, sizeof(cp));
@@ -802,9 +822,10 @@ void fill_combine(CombineParams& cp, int nmod, int P) {
         std::memcpy(cp.w[t], Mt.w, sizeof(Mt.w));
     }
     std::memcpy(cp.M, M.w, sizeof(M.w));
-    for (int l = 0; l < LIMBS; ++l) cp.halfM[l] = (M.w[l] >> 1) | (l + 1 < LIMBS ? (M.w[l + 1] << 31) : 0u);
-    cp.shift = std::max(0, M.bitlen() - 24);
-    cp.inv_mhi = 1.0f / (float)M.bits64(cp.shift);
+    // M / 2^(32 (L-2)) from its top three limbs, as the kernel forms X's
+    const int L = limbs_for(nmod);
+    const double m2 = (double)M.w[L - 1] * 4294967296.0 + (double)M.w[L - 2] + (double)M.w[L - 3] / 4294967296.0;
+    cp.inv_m2 = (float)(1.0 / m2);
 }
 
 template <int NL>
@@ -817,12 +838,15 @@ void launch_split_nl(bool kcontig, const double* X, int64_t ld, int64_t rows, in
 
 void launch_split(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps,
                   int64_t k_pad, int64_t rows_pad, uint16_t* out, const SplitParams& sp, dim3 grid, cudaStream_t st) {
-    switch (sp.limbs) {  // P <= 71: 4 limbs; <= 89: 5; <= 107: 6; else 7
-        case 1: case 2: case 3: case 4: launch_split_nl<4>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
-        case 5: launch_split_nl<5>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
-        case 6: launch_split_nl<6>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
-        default: launch_split_nl<7>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st); break;
+#define CGB_SPLIT_NL(NL) launch_split_nl<NL>(kcontig, X, ld, rows, k, exps, k_pad, rows_pad, out, sp, grid, st)
+    switch (sp.limbs) {  // P <= 64: 5 limbs; <= 77: 6; <= 90: 7; <= 103: 8; else 9
+        case 1: case 2: case 3: case 4: case 5: CGB_SPLIT_NL(5); break;
+        case 6: CGB_SPLIT_NL(6); break;
+        case 7: CGB_SPLIT_NL(7); break;
+        case 8: CGB_SPLIT_NL(8); break;
+        default: CGB_SPLIT_NL(9); break;
     }
+#undef CGB_SPLIT_NL
 }
 
 template <int NL>
@@ -842,24 +866,17 @@ void launch_split_cplx_nl(bool kcontig, bool bside, const double2* X, int64_t ld
 void launch_split_cplx(bool kcontig, bool bside, const double2* X, int64_t ld, int64_t rows, int64_t k,
                        const int* exps, int64_t kh, int64_t rows_pad, int64_t slice_rows, int conj, uint16_t* out,
                        const SplitParams& sp, dim3 grid, cudaStream_t st) {
+#define CGB_SPLITC_NL(NL) \
+    launch_split_cplx_nl<NL>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st)
     switch (sp.limbs) {
-        case 1: case 2: case 3: case 4:
-            launch_split_cplx_nl<4>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
-            break;
-        case 5:
-            launch_split_cplx_nl<5>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
-            break;
-        case 6:
-            launch_split_cplx_nl<6>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
-            break;
-        default:
-            launch_split_cplx_nl<7>(kcontig, bside, X, ld, rows, k, exps, kh, rows_pad, slice_rows, conj, out, sp, grid, st);
-            break;
+        case 1: case 2: case 3: case 4: case 5: CGB_SPLITC_NL(5); break;
+        case 6: CGB_SPLITC_NL(6); break;
+        case 7: CGB_SPLITC_NL(7); break;
+        case 8: CGB_SPLITC_NL(8); break;
+        default: CGB_SPLITC_NL(9); break;
     }
+#undef CGB_SPLITC_NL
 }
-
-// Limbs the reconstruction needs: sum_t r_t w_t < nmod * 255 * M.
-int limbs_for(int nmod) { return (modulus_product(nmod).bitlen() + 13 + 31) / 32; }
 
 struct Workspace {
     DeviceBuffer resA, resB, expA, expB, part, R, stats, err;
@@ -942,11 +959,11 @@ int launch_gemm(const void* resA, const void* resB, int64_t k_pad, const GemmPar
 template <bool RESIDUAL>
 void launch_combine_t(const CombineParams& cp, int limbs, unsigned grid, cudaStream_t st) {
     switch (limbs) {
-        case 1: case 2: case 3: case 4: combine_kernel<4, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
-        case 5: combine_kernel<5, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
-        case 6: combine_kernel<6, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
-        case 7: combine_kernel<7, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
-        default: combine_kernel<8, RESIDUAL><<<grid, 512, 0, st>>>(cp); break;
+        case 4: combine_kernel<4, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
+        case 5: combine_kernel<5, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
+        case 6: combine_kernel<6, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
+        case 7: combine_kernel<7, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
+        default: combine_kernel<8, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
     }
 }
 
@@ -986,7 +1003,7 @@ void fill_gemm(GemmParams& p, int nmod, int64_t m_pad, int64_t n_pad, int64_t k_
 struct Plan {
     int nmod = 0, P = 0;
     double spread = 0.0;
-    bool fallback = false;
+    bool exact = false;  // every input bit kept: the product is exact
 };
 
 int finish_info(cosma_gpu_ozaki_info* info, Workspace* w, const Plan& pl, int64_t kb_count) {
@@ -997,6 +1014,7 @@ int finish_info(cosma_gpu_ozaki_info* info, Workspace* w, const Plan& pl, int64_
     info->slices = pl.nmod;
     info->products = pl.nmod;
     info->fraction_bits = pl.P;
+    info->exact_product = pl.exact ? 1 : 0;
     info->groups = pl.nmod * (int)((kb_count + KB_PER_CHUNK - 1) / KB_PER_CHUNK);
     info->spread_bits = pl.spread;
     info->prep_ms += prep;
@@ -1056,7 +1074,8 @@ int dgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
         if (info) info->fallback_native = 1;
         return native_gemm(g, st);
     }
-    CGB_CHECK(choose(nmod_req, pl.spread, k, &pl.nmod, &pl.P));
+    CGB_CHECK(choose(nmod_req, pl.spread, k, &pl.nmod, &pl.P, std::max(hs.exact_bits[0], hs.exact_bits[1])));
+    pl.exact = pl.P >= std::max(hs.exact_bits[0], hs.exact_bits[1]);
 
     // 2. residue matrices
     const size_t resA_bytes = (size_t)pl.nmod * m_pad * k_pad * 2, resB_bytes = (size_t)pl.nmod * n_pad * k_pad * 2;
@@ -1143,7 +1162,8 @@ int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
         if (info) info->fallback_native = 1;
         return native_gemm(g, st);
     }
-    CGB_CHECK(choose(nmod_req, pl.spread, 2 * k, &pl.nmod, &pl.P));
+    CGB_CHECK(choose(nmod_req, pl.spread, 2 * k, &pl.nmod, &pl.P, std::max(hs.exact_bits[0], hs.exact_bits[1])));
+    pl.exact = pl.P >= std::max(hs.exact_bits[0], hs.exact_bits[1]);
 
     CGB_CHECK(w->resA.reserve((size_t)pl.nmod * m_pad * k_pad * 2, st));
     CGB_CHECK(w->resB.reserve((size_t)pl.nmod * n_pad * k_pad * 2, st));
@@ -1213,7 +1233,7 @@ extern "C" int cosma_gpu_dgemm_ozaki2_residual(char transa, char transb, int64_t
                                                int64_t ldo, void* stream, cosma_gpu_ozaki_info* info) {
     using namespace cgb;
     clear_error();
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     const int opa = parse_op(transa), opb = parse_op(transb);
     if (opa < 0 || opb < 0 || opa == 2 || opb == 2)
         return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2 residual: op must be N or T");
@@ -1235,11 +1255,12 @@ extern "C" int cosma_gpu_dgemm_ozaki2_residual(char transa, char transb, int64_t
     return oz2::dgemm(g, moduli, (cudaStream_t)stream, info, &r);
 }
 
-extern "C" int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int moduli, int* nmod, int* fraction_bits) {
+extern "C" int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int exact_bits, int moduli, int* nmod,
+                                       int* fraction_bits) {
     cgb::clear_error();
     if (k < 1 || !nmod || !fraction_bits)
         return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "ozaki2_choose: k >= 1 and output pointers needed");
-    return cgb::oz2::choose(moduli, spread_bits, k, nmod, fraction_bits);
+    return cgb::oz2::choose(moduli, spread_bits, k, nmod, fraction_bits, exact_bits > 0 ? exact_bits : (1 << 30));
 }
 
 namespace cgb {
@@ -1250,7 +1271,7 @@ int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_o
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: buffers must be 8-byte aligned");
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: m and n are limited to 2^24");
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     // one pass is exact for k up to KMAX (the split grid's K extent); longer
     // K runs in passes accumulated through C (beta = 1 after the first)
     GemmDesc c = g;
@@ -1270,7 +1291,7 @@ int ozaki2_zgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_o
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: complex buffers must be 16-byte aligned");
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 23)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: m is limited to 2^24 and n to 2^23 (complex)");
-    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    if (info) *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
     const int64_t kmax = oz2::KMAX / 2;  // each complex term is two real terms
     GemmDesc c = g;
     for (int64_t k0 = 0; k0 < g.k; k0 += kmax) {

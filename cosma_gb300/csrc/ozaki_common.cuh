@@ -38,14 +38,16 @@ struct Schedule {
 struct RowState {
     int emax;     // floor(log2 max |x|) over the elements seen, INT_MIN/2 if none
     float mass;   // sum of 2^(floor(log2|x|) - emax)
+    int lsbmin = 1 << 30;  // lowest weight of a set significand bit (log2), where tracked
 };
 
 __device__ __forceinline__ float pow2f(int e) {  // 2^e as float, 0 below the normal range
     return e < -126 ? 0.0f : __int_as_float((127 + e) << 23);
 }
 
-// floor(log2|x|) of a finite nonzero double from its bits; sets *bad for Inf/NaN.
-__device__ __forceinline__ bool element_log2(double x, int* lb, unsigned* bad) {
+// floor(log2|x|) of a finite nonzero double from its bits, and the log2
+// weight of its lowest set significand bit; sets *bad for Inf/NaN.
+__device__ __forceinline__ bool element_log2(double x, int* lb, unsigned* bad, int* lsb = nullptr) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x);
     int ef = (int)((b >> 52) & 0x7FF);
     unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
@@ -53,30 +55,35 @@ __device__ __forceinline__ bool element_log2(double x, int* lb, unsigned* bad) {
     if (ef == 0) {
         if (frac == 0) return false;
         *lb = (63 - __clzll((long long)frac)) - 1074;
+        if (lsb) *lsb = __ffsll((long long)frac) - 1 - 1074;
         return true;
     }
     *lb = ef - 1023;
+    if (lsb) *lsb = __ffsll((long long)(frac | (1ull << 52))) - 1 + ef - 1075;
     return true;
 }
 
-__device__ __forceinline__ void state_add(RowState& s, int lb) {
+__device__ __forceinline__ void state_add(RowState& s, int lb, int lsb = 1 << 30) {
     if (lb > s.emax) {
         s.mass = s.mass * pow2f(s.emax - lb) + 1.0f;
         s.emax = lb;
     } else {
         s.mass += pow2f(lb - s.emax);
     }
+    s.lsbmin = min(s.lsbmin, lsb);
 }
 __device__ __forceinline__ RowState state_merge(RowState a, RowState b) {
     RowState r;
     r.emax = max(a.emax, b.emax);
     r.mass = a.mass * pow2f(a.emax - r.emax) + b.mass * pow2f(b.emax - r.emax);
+    r.lsbmin = min(a.lsbmin, b.lsbmin);
     return r;
 }
 
 struct Stats {
     unsigned nonfinite;
-    float spread[2];  // max over rows of log2(2k / mass) for A rows / B columns
+    float spread[2];    // max over rows of log2(2k / mass) for A rows / B columns
+    int exact_bits[2];  // max over rows of E - (lowest set bit): fraction bits that keep every element exact
 };
 
 // Finishes one row: writes the scale exponent (E = emax + 1, 0 for zero
@@ -87,6 +94,7 @@ __device__ __forceinline__ void finish_row(RowState s, int64_t k, int* exp_out, 
         return;
     }
     *exp_out = s.emax + 1;
+    if (s.lsbmin < (1 << 30)) atomicMax(&st->exact_bits[which], s.emax + 1 - s.lsbmin);
     float spread = log2f(2.0f * (float)k / s.mass);
     if (spread < 0.0f) spread = 0.0f;
     atomicMax((int*)&st->spread[which], __float_as_int(spread));  // non-negative floats order as ints

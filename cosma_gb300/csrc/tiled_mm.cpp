@@ -167,7 +167,7 @@ int tmm_gemm(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int64_t m, int
     const bool dA = is_device_ptr(A), dB = is_device_ptr(B), dC = is_device_ptr(C);
     const bool trivial = (k == 0) || is_zero(alpha, sc);
     cosma_gpu_ozaki_info* info = &h->last_info;
-    *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0};
+    *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
 
     if (trivial && is_one(beta, sc)) return COSMA_GPU_SUCCESS;  // C unchanged
     if (dC && (trivial || (dA && dB))) {  // everything already in HBM

@@ -78,6 +78,7 @@ typedef struct cosma_gpu_ozaki_info {
     double prep_ms;      /* scaling + slicing kernels (CUDA events)         */
     double gemm_ms;      /* slice-product GEMM kernel (CUDA events)         */
     int fraction_bits;   /* fixed-point fraction bits of the operands       */
+    int exact_product;   /* 1: every input bit kept, the product is exact   */
 } cosma_gpu_ozaki_info;
 
 /* ----------------------------------------------------- Tiled-MM interface */
@@ -199,9 +200,12 @@ int cosma_gpu_zgemm_ozaki_device(char transa, char transb, int64_t m, int64_t n,
  * modulus), and the exact integer product is rebuilt by the Chinese
  * remainder theorem and rounded once to FP64.  moduli <= 0 sizes the count
  * (and P) from the inputs' exponent spread; explicit counts run from 2 to
- * 28, and P is the largest the count allows for this k.  In *info,
- * `slices` and `products` report the modulus count, `groups` the FP32
- * accumulator drains per output tile, `fraction_bits` P.  Inf/NaN inputs
+ * 28, and P is the largest the count allows for this k.  The automatic
+ * count is the fewest moduli that either keep every bit of the inputs (the
+ * product is then exact and C correctly rounded) or meet the accuracy rule
+ * for the inputs' exponent spread.  In *info, `slices` and `products` report
+ * the modulus count, `groups` the FP32 accumulator drains per output tile,
+ * `fraction_bits` P and `exact_product` whether every input bit was kept.  Inf/NaN inputs
  * run the native kernel (fallback_native = 1).  k beyond 4,194,240 runs in
  * passes accumulated through C. */
 int cosma_gpu_dgemm_ozaki2_device(char transa, char transb, int64_t m, int64_t n, int64_t k,
@@ -222,10 +226,15 @@ int cosma_gpu_dgemm_ozaki2_residual(char transa, char transb, int64_t m, int64_t
                                     const double* Ct, int64_t ldt, int moduli, double* E, double* Rx,
                                     int64_t ldo, void* stream, cosma_gpu_ozaki_info* info);
 /* The modulus count and fraction bits P that cosma_gpu_dgemm_ozaki2_device
- * uses for depth k (2k for the complex form) and the measured exponent
- * spread of the operands (the info record's spread_bits); moduli > 0 fixes
- * the count as in the GEMM call.  Host-only: touches no device. */
-int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int moduli, int* nmod, int* fraction_bits);
+ * uses for depth k (2k for the complex form), the measured exponent spread
+ * of the operands (the info record's spread_bits) and exact_bits, the
+ * fraction bits that keep every input bit (max over rows and columns of the
+ * scale exponent minus the weight of the lowest set bit; <= 0: unknown):
+ * the fewer moduli of the two that meet the accuracy rule or keep every bit.
+ * moduli > 0 fixes the count as in the GEMM call.  Host-only: touches no
+ * device. */
+int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int exact_bits, int moduli, int* nmod,
+                            int* fraction_bits);
 /* The same for complex double (interleaved re/im, op N, T or C): both parts
  * of C come out of one modular GEMM of depth 2k per modulus (four real
  * products per complex one), each part exact before its one rounding.

@@ -30,7 +30,9 @@ from .ozaki import row_exponents
 # Pairwise coprime moduli, largest first: 255 = 3*5*17, 254 = 2*127,
 # 253 = 11*23, 247 = 13*19, the rest primes.  Balanced residues lie in
 # [-127, 127], so every residue is exact in BF16 and 1024 products of two
-# residues sum below 2^24 (exact in the FP32 accumulator).
+# residues sum below 2^24 (exact in the FP32 accumulator).  The automatic
+# count is the fewer of the accuracy rule's and the count that keeps every
+# input bit (then the product is exact and C correctly rounded).
 MODULI = (255, 254, 253, 251, 247, 241, 239, 233, 229, 227, 223, 211, 199, 197, 193, 191, 181, 179, 173, 167,
           163, 157, 151, 149, 139, 137, 131, 113)
 MAX_MODULI = len(MODULI)
@@ -50,13 +52,41 @@ def max_fraction_bits(nmod, k):
     return (product_bits(nmod) - 1 - ceil_log2(k) - 2) // 2
 
 
-def choose_moduli(p_req, k):
-    """Smallest modulus count whose product admits P >= p_req; returns (N, P)."""
+def _fewest(p_req, k):
     for nmod in range(2, MAX_MODULI + 1):
-        P = max_fraction_bits(nmod, k)
-        if P >= p_req:
-            return nmod, P
-    return MAX_MODULI, max_fraction_bits(MAX_MODULI, k)
+        if max_fraction_bits(nmod, k) >= p_req:
+            return nmod
+    return MAX_MODULI + 1
+
+
+def choose_moduli(p_req, k, exact_bits=None):
+    """The automatic choice: the fewer moduli of those whose product admits
+    P >= p_req (the accuracy rule) and those that keep every input bit
+    (P >= exact_bits); returns (N, P) with P the largest N allows (<= 116)."""
+    nmod = _fewest(p_req, k)
+    if exact_bits is not None:
+        nmod = min(nmod, _fewest(max(int(exact_bits), 1), k))
+    nmod = min(nmod, MAX_MODULI)
+    return nmod, min(max_fraction_bits(nmod, k), 116)
+
+
+def exact_fraction_bits(X):
+    """Max over the rows of X of E_i minus the weight (log2) of the lowest set
+    significand bit in the row: the fraction bits that represent every
+    element exactly (0 for an all-zero X)."""
+    X = np.asarray(X, dtype=np.float64)
+    E = row_exponents(X)
+    b = X.view(np.uint64)
+    ef = ((b >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    frac = b & np.uint64(0xFFFFFFFFFFFFF)
+    M = np.where(ef == 0, frac, frac | np.uint64(1 << 52))
+    eu = np.where(ef == 0, -1074, ef - 1075)
+    low = M & (~M + np.uint64(1))                      # lowest set bit of M
+    tz = np.log2(np.where(M == 0, 1, low).astype(np.float64)).astype(np.int64)
+    lsb = np.where(M == 0, 1 << 30, eu + tz)
+    rowmin = lsb.min(axis=1) if X.shape[1] else np.full(X.shape[0], 1 << 30)
+    bits = np.where(rowmin < (1 << 30), E - rowmin, 0)
+    return int(bits.max()) if bits.size else 0
 
 
 def scaled_integers(X, E, P):
@@ -171,9 +201,10 @@ def ozaki2_zgemm_sampled(ta, tb, A, B, P, rows, cols):
 
 
 def residues(v, p):
-    """Balanced residue of the Python int v modulo p, as the split kernel stores it."""
-    r = v % p
-    return r - p if r > p // 2 else r
+    """Balanced residue of the Python int v modulo p, as the split kernel
+    stores it: ((v + h) mod p) - h with h = floor(p / 2), in [-h, p - 1 - h]."""
+    h = p // 2
+    return (v + h) % p - h
 
 
 def crt_reconstruct(res, nmod):

@@ -43,6 +43,29 @@ def test_unpack_real_bit_exact(native_lib, cuda, alpha, beta):
     assert got.tobytes() == ref.tobytes()
 
 
+@pytest.mark.parametrize("alpha,beta", [(2.0, 0.5), (0.25, 4.0), (1.0, 2.0 ** -1000), (2.0 ** 1000, 1.0)])
+def test_unpack_power_of_two_scales_at_the_range_edges(native_lib, cuda, alpha, beta):
+    """Power-of-two alpha / beta scale by moving the exponent field; values whose
+    scaled exponent leaves the normal range (subnormals, overflow to Inf, the
+    smallest normals) must still round exactly as the FP64 multiply does."""
+    from cosma_gb300 import unpack
+    rows, cols = 64, 9
+    rng = np.random.default_rng(9)
+    S = oracle.normal((rows, cols), 5)
+    D0 = oracle.normal((rows, cols), 6)
+    edge = np.array([0.0, -0.0, 5e-324, -7e-322, 2.2250738585072014e-308, 4.4e-308, 1.7e308, -1.2e308,
+                     np.inf, -np.inf, 3.0e-300, 1e-310, 2.0 ** -1022 * 3, 1.0, 0.75, 2.0 ** 1023])
+    for X in (S, D0):
+        X[:edge.size, 0] = edge
+        X[:edge.size, 1] = -edge[::-1]
+        X[:, 2] = rng.choice(edge, rows)
+    dS, dD = to_dev(S), to_dev(D0)
+    unpack(rows, cols, alpha, dS, rows, beta, dD, rows, scalar="d")
+    got = from_dev(dD, rows, cols)
+    ref = oracle.unpack(alpha, S, beta, D0.copy(order="F"))
+    assert got.tobytes() == ref.tobytes()
+
+
 def test_unpack_complex_bit_exact(native_lib, cuda):
     from cosma_gb300 import unpack
     rows, cols = 65, 33

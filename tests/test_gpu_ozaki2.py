@@ -49,14 +49,22 @@ def test_bit_exact_against_restatement(native_lib, cuda, ta, tb, m, n, k, N):
 
 
 def test_automatic_modulus_count(native_lib, cuda):
+    """The automatic count is the host rule on the measured spread and exact
+    bits; where it keeps every input bit the result is the correctly rounded
+    product."""
     import cosma_gb300 as cg
     m, n, k = 48, 40, 300
     for phi in (0, 8, 32):
         A = oracle.exp_spread((m, k), 10 + phi, phi)
         B = oracle.exp_spread((k, n), 20 + phi, phi)
         got, info = _run("N", "N", m, n, k, A, B)
-        assert (info["slices"], info["fraction_bits"]) == cg.ozaki2_choose(k, info["spread_bits"])
+        exact = max(o2.exact_fraction_bits(A), o2.exact_fraction_bits(B.T))
+        assert (info["slices"], info["fraction_bits"]) == cg.ozaki2_choose(k, info["spread_bits"], exact_bits=exact)
+        assert info["exact_product"] == int(info["fraction_bits"] >= exact)
         np.testing.assert_array_equal(got, o2.ozaki2_gemm("N", "N", A, B, info["fraction_bits"]))
+        if info["exact_product"]:
+            hi, lo, ab = oracle.gemm_dd("N", "N", A, B)
+            np.testing.assert_array_equal(got, hi + lo)  # correctly rounded
 
 
 @pytest.mark.parametrize("k", [1024, 1025, 5000, 70000])

@@ -85,9 +85,27 @@ def test_host_plan_matches_the_restatement(native_lib):
                 with pytest.raises(cg.CosmaGpuError):
                     cg.ozaki2_choose(k, 0.0, nmod)
                 continue
-            assert cg.ozaki2_choose(k, 0.0, nmod) == (nmod, min(P, 120))
+            assert cg.ozaki2_choose(k, 0.0, nmod) == (nmod, min(P, 116))
         for spread in (0.0, 5.2, 12.0, 40.0):
             lk = math.log2(k)
             want = math.ceil(max(60.0, 65.0 + 0.85 * (spread - 3.3) - (lk - 8.0)))
-            nmod, P = o2.choose_moduli(want, k)
-            assert cg.ozaki2_choose(k, spread) == (nmod, P)
+            assert cg.ozaki2_choose(k, spread) == o2.choose_moduli(want, k)
+            for exact in (1, 53, 61, 85, 200):
+                assert cg.ozaki2_choose(k, spread, exact_bits=exact) == o2.choose_moduli(want, k, exact)
+
+
+def test_exact_fraction_bits():
+    X = np.array([[0.75, -0.5, 0.0], [2.0 ** -60, 1.0, 3.0]])
+    # row 0: E = 0, lowest set bits 2^-2 (0.75), 2^-1 -> 2; row 1: E = 2, lowest 2^-60 -> 62
+    assert o2.exact_fraction_bits(X) == 62
+    assert o2.exact_fraction_bits(np.zeros((3, 4))) == 0
+    U = oracle.uniform((50, 200), 3)  # numpy uniforms are multiples of 2^-53
+    assert o2.exact_fraction_bits(U) <= 53
+    # with P >= the exact bits every scaled integer is exact: no rounding happened
+    Y = oracle.exp_spread((6, 40), 5, 8)
+    P = o2.exact_fraction_bits(Y)
+    E = oracle.ozaki.row_exponents(Y)
+    Z = o2.scaled_integers(Y, E, P)
+    for i in range(Y.shape[0]):
+        for l in range(Y.shape[1]):
+            assert math.ldexp(int(Z[i, l]), int(E[i]) - P) == Y[i, l]
