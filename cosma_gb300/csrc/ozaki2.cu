@@ -756,10 +756,15 @@ int ceil_log2(int64_t k) {
 int max_fraction_bits(int nmod, int64_t k) { return (modulus_product(nmod).bitlen() - 1 - ceil_log2(k) - 2) / 2; }
 
 // Fraction bits the requested accuracy needs for inputs with this exponent
-// spread: the calibrated width of the slice form (oz::required_fraction_bits)
-// plus COSMA_GPU_OZAKI2_EXTRA_BITS.
+// spread: the width calibrated for the slice form on sampled entries
+// (oz::required_fraction_bits) plus 16 bits (COSMA_GPU_OZAKI2_EXTRA_BITS).
+// Checking every entry of 16384^3 products showed the sampled calibration
+// short for the worst-cancelling entries: u*2^e inputs with phi = 8 had 5,499
+// entries above 1e-15 relative error at P = 65 (max 4e-11), phi = 32 had
+// 1,266 at P = 69 (max 8e-13); the input-rounding error falls by 2^-16 for
+// 16 more bits, below the target for both.
 int requested_fraction_bits(double spread, int64_t k) {
-    static const long long extra = env_ll("COSMA_GPU_OZAKI2_EXTRA_BITS", 0);
+    static const long long extra = env_ll("COSMA_GPU_OZAKI2_EXTRA_BITS", 16);
     return (int)std::ceil(oz::required_fraction_bits(spread, k)) + (int)extra;
 }
 

@@ -88,7 +88,7 @@ def test_host_plan_matches_the_restatement(native_lib):
             assert cg.ozaki2_choose(k, 0.0, nmod) == (nmod, min(P, 116))
         for spread in (0.0, 5.2, 12.0, 40.0):
             lk = math.log2(k)
-            want = math.ceil(max(60.0, 65.0 + 0.85 * (spread - 3.3) - (lk - 8.0)))
+            want = math.ceil(max(60.0, 65.0 + 0.85 * (spread - 3.3) - (lk - 8.0))) + 16
             assert cg.ozaki2_choose(k, spread) == o2.choose_moduli(want, k)
             for exact in (1, 53, 61, 85, 200):
                 assert cg.ozaki2_choose(k, spread, exact_bits=exact) == o2.choose_moduli(want, k, exact)
