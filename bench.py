@@ -442,7 +442,8 @@ def cfg_grouped(steps, warmup, count=10000):
     """10,000 independent FP64 GEMMs, m, n, k log-uniform integers in [16, 1024],
     transa/transb uniform in {N, T}, U[-1, 1] entries: one persistent grouped
     launch (autotuned, CUDA graph) in native FP64 and in the digit-slice Ozaki
-    form, against a loop of per-problem drop-in calls."""
+    form and in the Chinese-remainder form, against a loop of per-problem
+    drop-in calls."""
     import torch
 
     import cosma_gb300 as cg
@@ -519,6 +520,17 @@ def cfg_grouped(steps, warmup, count=10000):
     oslices = oplan.slices()
     acc_oz = accuracy(picks)
     oplan.close()
+    # the Chinese-remainder form: one modulus count for the batch
+    t0 = time.perf_counter()
+    cplan = cg.GroupedPlan(probs, method="ozaki2", autotune=True)
+    cplan_s = time.perf_counter() - t0
+    for _ in range(max(warmup, 3)):
+        cplan.run(stream=s)
+    cms, _ = cuda_ms(lambda: cplan.run(stream=s), s, steps)
+    cinfo = cplan.info()
+    cmods = [x for x in cplan.slices() if x]
+    acc_crt = accuracy(picks)
+    cplan.close()
     # loop of per-problem drop-in calls (the reference's way of running a batch)
     torch.cuda.synchronize()
     l0 = time.perf_counter()
@@ -533,17 +545,37 @@ def cfg_grouped(steps, warmup, count=10000):
     bms, _ = cuda_ms(lambda: cg.gemm_device("N", "N", big, big, big, 1.0, X, big, X, big, 0.0, Y, big,
                                             method="native", stream=s), s, 1)
     native_peak = 2.0 * big ** 3 / (bms * 1e-3) / 1e12
-    # e2e: the batch from host memory - inputs copied in, the grouped launch, C copied out
+    # e2e: the batch from host memory - inputs copied in, the grouped launch, C
+    # copied out, the copies by the library's copy kernel (COSTA pack, op N)
+    # reading and writing the pinned host arrays in place
     hA, hB = dA.cpu().pin_memory(), dB.cpu().pin_memory()
     hC = torch.empty(dC.numel(), dtype=torch.float64).pin_memory()
-    plan = cg.GroupedPlan(probs, method="ozaki", autotune=False)
+    route = cg.host_copy_route(hA)
+
+    def flat_copy(dst, src, count_):
+        rows = 1 << 20
+        main = count_ // rows * rows
+        if main:
+            cg.pack("N", rows, main // rows, src, rows, dst, rows, stream=s)
+        if count_ - main:
+            cg.pack("N", count_ - main, 1, src.data_ptr() + 8 * main, count_ - main, dst.data_ptr() + 8 * main,
+                    count_ - main, stream=s)
+
+    plan = cg.GroupedPlan(probs, method="ozaki2", autotune=False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(3):
-        dA.copy_(hA, non_blocking=True)
-        dB.copy_(hB, non_blocking=True)
+        if route == 2:
+            flat_copy(dA, hA, dA.numel())
+            flat_copy(dB, hB, dB.numel())
+        else:
+            dA.copy_(hA, non_blocking=True)
+            dB.copy_(hB, non_blocking=True)
         plan.run(stream=s)
-        hC.copy_(dC, non_blocking=True)
+        if route == 2:
+            flat_copy(hC, dC, dC.numel())
+        else:
+            hC.copy_(dC, non_blocking=True)
         torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / 3
     plan.close()
@@ -559,6 +591,8 @@ def cfg_grouped(steps, warmup, count=10000):
     torch.cuda.empty_cache()
     value = useful / (ms * 1e-3) / 1e12
     oval = useful / (oms * 1e-3) / 1e12
+    cval = useful / (cms * 1e-3) / 1e12
+    pk, pk_kind = peaks()
     return {"metric": f"grouped FP64 GEMM TFLOP/s ({count:,} uneven problems, one launch)", "value": value,
             "unit": UNIT, "steps": steps, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64",
             "data": "synthetic U[-1,1], seeded",
@@ -571,6 +605,13 @@ def cfg_grouped(steps, warmup, count=10000):
                                  "speedup_vs_native_grouped": ms / oms, "tiles": oinfo["tiles"],
                                  "fp8_flops_issued": oinfo["padded_flops"],
                                  "slices_min_max": [min(oslices), max(oslices)], "accuracy": acc_oz},
+            "crt_form": {"tflops": cval, "ms": cms, "plan_build_s": cplan_s, "speedup_vs_native_grouped": ms / cms,
+                         "speedup_vs_split_form": oms / cms, "tiles": cinfo["tiles"], "moduli": max(cmods),
+                         "bf16_flops_issued": cinfo["padded_flops"],
+                         "bf16_tflops_issued": cinfo["padded_flops"] / (cms * 1e-3) / 1e12,
+                         "bf16_frac_of_sustained": cinfo["padded_flops"] / (cms * 1e-3) / 1e12
+                         / pk["bf16_tflops_sustained"],
+                         "peak_kind": pk_kind, "accuracy": acc_crt},
             "accuracy": acc_native,
             "roofline": {"bound": "fp64", "achieved": value, "peak": native_peak, "unit": "TFLOP/s",
                          "frac": value / native_peak, "traffic": None, "kernel": "grouped_dmma_kernel",
@@ -578,7 +619,9 @@ def cfg_grouped(steps, warmup, count=10000):
                          "frac_of_nominal_fp64": value / FP64_NOMINAL_TFLOPS},
             "e2e": {"value": useful / e2e_s / 1e12, "unit": UNIT,
                     "h2d_bytes_per_step": int(8 * (sa[-1] + sb[-1])), "d2h_bytes_per_step": int(8 * sc[-1]),
-                    "entry": "grouped plan (Ozaki form) with the batch copied in from and out to pinned host memory",
+                    "entry": "grouped plan (Chinese-remainder form) with the batch copied in from and out to pinned "
+                             "host memory" + (" by the library's in-place copy kernel (costa_gpu_pack reading / "
+                                              "writing host memory)" if route == 2 else " (cudaMemcpyAsync)"),
                     "ms_per_step": e2e_s * 1e3},
             "cpu_baseline": {"value": cpu_flops / cpu_s / 1e12, "unit": UNIT, "cores": oracle.openblas_threads(),
                              "kind": "port", "sample": f"OpenBLAS DGEMM per problem on 500 of the {count:,} problems"},

@@ -324,7 +324,7 @@ def multiply_using_layout(transa, transb, alpha, a: BlockLayout, b: BlockLayout,
 
 class GroupedPlan:
     """A grouped FP64 GEMM over many device problems, one persistent launch
-    replayed from a CUDA graph (method "native" or "ozaki").  `problems` is a list of tuples
+    replayed from a CUDA graph (method "native", "ozaki" or "ozaki2").  `problems` is a list of tuples
     (transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) with device
     buffers (torch tensors or raw addresses)."""
 
@@ -348,7 +348,9 @@ class GroupedPlan:
         return inf.as_dict()
 
     def slices(self):
-        """Planned slice count per problem (Ozaki plans; 0 where not sliced)."""
+        """Planned slice count per problem of an "ozaki" plan, the batch's
+        modulus count for each problem of an "ozaki2" plan (0 where a problem
+        is not on the grouped path, and for native plans)."""
         out = (C.c_int * max(1, len(self._keep)))()
         N.check(self.lib.cosma_gpu_grouped_plan_slices(self._p, out))
         return list(out)[:len(self._keep)]

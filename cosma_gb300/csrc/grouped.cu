@@ -186,7 +186,8 @@ struct cosma_gpu_grouped_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t capture_stream = nullptr;
-    cosma_gpu_oz_grouped_plan* oz = nullptr;  // the Ozaki-split form, when chosen
+    cosma_gpu_oz_grouped_plan* oz = nullptr;    // the Ozaki-split form, when chosen
+    cosma_gpu_oz2_grouped_plan* oz2 = nullptr;  // the Chinese-remainder form, when chosen
 };
 
 namespace cgb {
@@ -360,20 +361,22 @@ cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count, con
                                                       int autotune, void* stream) {
     using namespace cgb;
     clear_error();
-    if (method != COSMA_GPU_METHOD_AUTO && method != COSMA_GPU_METHOD_NATIVE && method != COSMA_GPU_METHOD_OZAKI) {
-        set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "grouped: the native FP64 and Ozaki methods are implemented");
+    if (method != COSMA_GPU_METHOD_AUTO && method != COSMA_GPU_METHOD_NATIVE && method != COSMA_GPU_METHOD_OZAKI &&
+        method != COSMA_GPU_METHOD_OZAKI2) {
+        set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "grouped: the native FP64 and the two Ozaki methods are implemented");
         return nullptr;
     }
     if (count < 0 || (count > 0 && !problems)) {
         set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: bad problem array");
         return nullptr;
     }
-    if (method == COSMA_GPU_METHOD_OZAKI) {
+    if (method == COSMA_GPU_METHOD_OZAKI || method == COSMA_GPU_METHOD_OZAKI2) {
         auto* pl = new cosma_gpu_grouped_plan();
         pl->count = count;
         int s = COSMA_GPU_SUCCESS;
-        pl->oz = oz_grouped_create(count, problems, autotune, (cudaStream_t)stream, &s);
-        if (!pl->oz) {
+        if (method == COSMA_GPU_METHOD_OZAKI) pl->oz = oz_grouped_create(count, problems, autotune, (cudaStream_t)stream, &s);
+        else pl->oz2 = oz2_grouped_create(count, problems, autotune, (cudaStream_t)stream, &s);
+        if (!pl->oz && !pl->oz2) {
             delete pl;
             return nullptr;
         }
@@ -421,6 +424,7 @@ int cosma_gpu_grouped_plan_run(cosma_gpu_grouped_plan* pl, void* stream) {
     cgb::clear_error();
     if (!pl) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: null plan");
     if (pl->oz) return cgb::oz_grouped_run(pl->oz, (cudaStream_t)stream);
+    if (pl->oz2) return cgb::oz2_grouped_run(pl->oz2, (cudaStream_t)stream);
     if (pl->ntiles == 0) return COSMA_GPU_SUCCESS;
     CGB_CUDA(cudaGraphLaunch(pl->exec, (cudaStream_t)stream));
     return COSMA_GPU_SUCCESS;
@@ -430,6 +434,10 @@ int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* pl, cosma_gpu_grouped_in
     if (!pl || !info) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: null argument");
     if (pl->oz) {
         cgb::oz_grouped_info(pl->oz, info);
+        return COSMA_GPU_SUCCESS;
+    }
+    if (pl->oz2) {
+        cgb::oz2_grouped_info(pl->oz2, info);
         return COSMA_GPU_SUCCESS;
     }
     info->tiles = pl->ntiles;
@@ -445,6 +453,7 @@ int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* pl, cosma_gpu_grouped_in
 int cosma_gpu_grouped_plan_slices(cosma_gpu_grouped_plan* pl, int* slices) {
     if (!pl || !slices) return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "grouped: null argument");
     if (pl->oz) return cgb::oz_grouped_slices(pl->oz, slices);
+    if (pl->oz2) return cgb::oz2_grouped_slices(pl->oz2, slices);
     for (int i = 0; i < pl->count; ++i) slices[i] = 0;
     return COSMA_GPU_SUCCESS;
 }
@@ -452,6 +461,7 @@ int cosma_gpu_grouped_plan_slices(cosma_gpu_grouped_plan* pl, int* slices) {
 void cosma_gpu_grouped_plan_destroy(cosma_gpu_grouped_plan* pl) {
     if (!pl) return;
     if (pl->oz) cgb::oz_grouped_destroy(pl->oz);
+    if (pl->oz2) cgb::oz2_grouped_destroy(pl->oz2);
     if (pl->exec) cudaGraphExecDestroy(pl->exec);
     if (pl->graph) cudaGraphDestroy(pl->graph);
     if (pl->capture_stream) cudaStreamDestroy(pl->capture_stream);

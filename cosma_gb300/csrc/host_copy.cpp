@@ -198,6 +198,14 @@ bool direct_copy(void* dst, size_t dpitch, const void* src, size_t spitch, size_
 
 }  // namespace
 
+bool prepare_direct_host(void* p, size_t pitch, size_t width, size_t cols, bool write) {
+    const HostMem hm = host_mem(p);
+    if (hm != HostMem::Pageable && hm != HostMem::PinnedMapped) return false;
+    if (!host_direct()) return false;
+    if (hm == HostMem::Pageable) prefault(p, pitch, width, cols, write);
+    return true;
+}
+
 int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                 cudaStream_t s) {
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;

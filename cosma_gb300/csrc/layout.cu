@@ -164,16 +164,38 @@ __device__ __forceinline__ R apply_scale(const ScaleMode<R>& m, R s, R x) {
 // modes only choose how each (exact or rounded) product is formed, never the
 // result: a multiply by 1 or by a power of two is exact unless it leaves the
 // normal range, where mul_pow2 multiplies.
+//
+// Each thread takes four elements of a column, a block stride apart, and
+// issues all their loads before any arithmetic: GB300's FP64 pipe is narrow
+// (the multiply and add of one element cost about what its 24 bytes of HBM
+// traffic do), so the loads of the next elements must be in flight while the
+// FP64 work of the current ones runs.
 template <class R>
 __global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, ScaleMode<R> am, const R* __restrict__ src,
                                    int64_t lds, R beta, ScaleMode<R> bm, R* __restrict__ dst, int64_t ldd,
                                    int read_dst) {
-    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y)
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-            R v = apply_scale(am, alpha, src[i + j * lds]);
-            if (read_dst) v = add_rn(v, apply_scale(bm, beta, dst[i + j * ldd]));
-            dst[i + j * ldd] = v;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y) {
+        const R* s = src + j * lds;
+        R* d = dst + j * ldd;
+        for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < rows; i0 += 4 * stride) {
+            R x[4], y[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t i = i0 + q * stride;
+                x[q] = i < rows ? s[i] : R(0);
+                y[q] = (read_dst && i < rows) ? d[i] : R(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t i = i0 + q * stride;
+                if (i >= rows) break;
+                R v = apply_scale(am, alpha, x[q]);
+                if (read_dst) v = add_rn(v, apply_scale(bm, beta, y[q]));
+                d[i] = v;
+            }
         }
+    }
 }
 
 // complex: x*y = (xr*yr - xi*yi) + (xr*yi + xi*yr) i, every product and sum
@@ -282,14 +304,15 @@ int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, co
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "unpack: buffers must be aligned to the element size");
     const int read_dst = !(beta[0] == 0.0 && (!scalar_complex(sc) || beta[1] == 0.0));
     dim3 g = grid2d(rows, cols, 256);
+    dim3 g4 = grid2d(ceil_div(rows, 4), cols, 256);  // the real kernels take four elements per thread
     switch (sc) {
         case Scalar::D:
-            unpack_real_kernel<double><<<g, 256, 0, s>>>(rows, cols, alpha[0], scale_mode<double>(alpha[0]),
+            unpack_real_kernel<double><<<g4, 256, 0, s>>>(rows, cols, alpha[0], scale_mode<double>(alpha[0]),
                                                          (const double*)src, lds, beta[0], scale_mode<double>(beta[0]),
                                                          (double*)dst, ldd, read_dst);
             break;
         case Scalar::S:
-            unpack_real_kernel<float><<<g, 256, 0, s>>>(rows, cols, (float)alpha[0], scale_mode<float>((float)alpha[0]),
+            unpack_real_kernel<float><<<g4, 256, 0, s>>>(rows, cols, (float)alpha[0], scale_mode<float>((float)alpha[0]),
                                                         (const float*)src, lds, (float)beta[0],
                                                         scale_mode<float>((float)beta[0]), (float*)dst, ldd, read_dst);
             break;

@@ -83,13 +83,26 @@ __global__ void scale_kcontig_kernel(const double* __restrict__ X, int64_t ld, i
     const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x & 31;
     if (row >= rows) return;
-    RowState s{-(1 << 30), 0.0f};
+    // four independent states per lane keep four loads in flight
+    RowState q[4] = {{-(1 << 30), 0.0f}, {-(1 << 30), 0.0f}, {-(1 << 30), 0.0f}, {-(1 << 30), 0.0f}};
     unsigned bad = 0;
     const double* p = X + row * ld;
-    for (int64_t l = lane; l < k; l += 32) {
-        int lb, lsb;
-        if (element_log2(p[l], &lb, &bad, &lsb)) state_add(s, lb, lsb);
+    int64_t l = lane;
+    for (; l + 96 < k; l += 128) {
+        double x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = p[l + 32 * u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int lb, lsb;
+            if (element_log2(x[u], &lb, &bad, &lsb)) state_add(q[u], lb, lsb);
+        }
     }
+    for (; l < k; l += 32) {
+        int lb, lsb;
+        if (element_log2(p[l], &lb, &bad, &lsb)) state_add(q[0], lb, lsb);
+    }
+    RowState s = state_merge(state_merge(q[0], q[1]), state_merge(q[2], q[3]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         RowState t;
@@ -117,14 +130,29 @@ __global__ void scale_mcontig_partial_kernel(const double* __restrict__ X, int64
     const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= rows) return;
     const int64_t l0 = (int64_t)blockIdx.y * kchunk, l1 = min(k, l0 + kchunk);
-    RowState s{-(1 << 30), 0.0f};
+    // four independent states keep four loads of the row in flight
+    RowState q[4] = {{-(1 << 30), 0.0f}, {-(1 << 30), 0.0f}, {-(1 << 30), 0.0f}, {-(1 << 30), 0.0f}};
     unsigned bad = 0;
-    for (int64_t l = l0; l < l1; ++l) {
+    int64_t l = l0;
+    for (; l + 3 < l1; l += 4) {
         for (int c = 0; c < es; ++c) {
-            int lb, lsb;
-            if (element_log2(X[row * es + c + l * ld], &lb, &bad, &lsb)) state_add(s, lb, lsb);
+            double x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) x[u] = X[row * es + c + (l + u) * ld];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                int lb, lsb;
+                if (element_log2(x[u], &lb, &bad, &lsb)) state_add(q[u], lb, lsb);
+            }
         }
     }
+    for (; l < l1; ++l) {
+        for (int c = 0; c < es; ++c) {
+            int lb, lsb;
+            if (element_log2(X[row * es + c + l * ld], &lb, &bad, &lsb)) state_add(q[0], lb, lsb);
+        }
+    }
+    const RowState s = state_merge(state_merge(q[0], q[1]), state_merge(q[2], q[3]));
     if (bad) atomicOr(&st->nonfinite, 1u);
     pe[blockIdx.y * rows + row] = s.emax;
     pm[blockIdx.y * rows + row] = s.mass;
@@ -633,8 +661,9 @@ int scale_operand(bool kcontig, const double* X, int64_t ld, int64_t rows, int64
         scale_kcontig_kernel<<<(unsigned)ceil_div(rows, 8), 256, 0, st>>>(X, ld * es, rows, k * es, exps, st_dev,
                                                                           which);
     } else {
+        // enough K chunks for ~16 blocks per SM: each thread walks one row's chunk
         const int64_t row_blocks = ceil_div(rows, 256);
-        int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
+        int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (16 * num_sms()) / row_blocks), 64);
         nchunks = (int)std::min<int64_t>(nchunks, std::max<int64_t>(1, k / 64));
         const int64_t kchunk = ceil_div(k, nchunks);
         CGB_CHECK(part.reserve((size_t)nchunks * rows * 12, st));
@@ -1088,7 +1117,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // split scale_rows uses, so both entry points pick the same slice count).
 inline int mcontig_chunks(int64_t rows, int64_t k) {
     const int64_t row_blocks = ceil_div(rows, 256);
-    int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (4 * num_sms()) / row_blocks), 64);
+    int nchunks = (int)std::min<int64_t>(std::max<int64_t>(1, (16 * num_sms()) / row_blocks), 64);
     return (int)std::min<int64_t>(nchunks, std::max<int64_t>(1, k / 64));
 }
 

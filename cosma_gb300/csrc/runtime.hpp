@@ -6,7 +6,8 @@
 #include <cstdint>
 #include <mutex>
 
-struct cosma_gpu_oz_grouped_plan;  // grouped Ozaki plan (ozaki_grouped.cu)
+struct cosma_gpu_oz_grouped_plan;   // grouped Ozaki plan (ozaki_grouped.cu)
+struct cosma_gpu_oz2_grouped_plan;  // grouped Chinese-remainder plan (ozaki2_grouped.cu)
 
 namespace cgb {
 
@@ -156,6 +157,10 @@ int copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size
 // Whether the device copy kernel route is on (capable device, and
 // COSMA_GPU_HOST_DIRECT not OFF).
 bool host_direct_available();
+// Whether kernels may read and write the column-major host array at p in
+// place (pageable or mapped pinned memory on a host whose page tables the
+// device uses); pageable pages are faulted in on the host first.
+bool prepare_direct_host(void* p, size_t pitch, size_t width, size_t cols, bool write);
 
 // Grouped Ozaki-split FP64 GEMM (ozaki_grouped.cu), driven by the grouped
 // plan of grouped.cu when it is created with the Ozaki method.
@@ -165,6 +170,13 @@ int oz_grouped_run(cosma_gpu_oz_grouped_plan* pl, cudaStream_t st);
 void oz_grouped_destroy(cosma_gpu_oz_grouped_plan* pl);
 void oz_grouped_info(const cosma_gpu_oz_grouped_plan* pl, cosma_gpu_grouped_info* info);
 int oz_grouped_slices(const cosma_gpu_oz_grouped_plan* pl, int* out);
+cosma_gpu_oz2_grouped_plan* oz2_grouped_create(int count, const cosma_gpu_gemm_problem* problems, int autotune,
+                                               cudaStream_t st, int* status);
+int oz2_grouped_run(cosma_gpu_oz2_grouped_plan* pl, cudaStream_t st);
+void oz2_grouped_destroy(cosma_gpu_oz2_grouped_plan* pl);
+void oz2_grouped_info(const cosma_gpu_oz2_grouped_plan* pl, cosma_gpu_grouped_info* info);
+int oz2_grouped_slices(const cosma_gpu_oz2_grouped_plan* pl, int* out);
+int oz2_grouped_fraction_bits(const cosma_gpu_oz2_grouped_plan* pl, int* out);
 
 // Dispatches one device-pointer GEMM by method (handles the k == 0 /
 // alpha == 0 corner cases).  Defined in gemm_dispatch.cpp.

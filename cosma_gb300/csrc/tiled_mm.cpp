@@ -226,12 +226,19 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     }
     const int64_t ntm = ceil_div(m, tm), ntn = ceil_div(n, tn), ntk = trivial ? 1 : ceil_div(k, tk);
     const int64_t ntiles = ntm * ntn, nsteps = ntiles * ntk;
+    const bool keep_on_device = !dC && !copy_c_back;
+    // One step with the Chinese-remainder method: its reconstruction kernel
+    // writes (and, for beta != 0, reads) C in host memory directly where the
+    // device reaches it, so the write-back overlaps that kernel instead of
+    // following it as a separate copy, and no C slot is needed.
+    const bool crt = h->method == COSMA_GPU_METHOD_OZAKI2 && (sc == Scalar::D || sc == Scalar::Z);
+    const bool direct_c = crt && !dC && !keep_on_device && !trivial && nsteps == 1 &&
+                          prepare_direct_host(C, (size_t)ldc * es, (size_t)m * es, (size_t)n, true);
     for (int s = 0; s < R; ++s) {
         if (!dA && !trivial) CGB_CHECK(h->bufA[s].reserve((size_t)tm * tk * es, h->streams[0]));
         if (!dB && !trivial) CGB_CHECK(h->bufB[s].reserve((size_t)tk * tn * es, h->streams[0]));
-        if (!dC) CGB_CHECK(h->bufC[s].reserve((size_t)tm * tn * es, h->streams[0]));
+        if (!dC && !direct_c) CGB_CHECK(h->bufC[s].reserve((size_t)tm * tn * es, h->streams[0]));
     }
-    const bool keep_on_device = !dC && !copy_c_back;
     if (keep_on_device) CGB_CHECK(h->full_c.reserve((size_t)m * n * es, h->streams[0]));
     CGB_CUDA(cudaDeviceSynchronize());  // buffers from any earlier call are idle
 
@@ -256,7 +263,7 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
         l0 = kt * tk; kk = trivial ? 0 : std::min(tk, k - l0);
     };
     auto cdev_of = [&](int64_t step, int64_t i0, int64_t j0, int64_t& cld) -> char* {
-        if (dC) { cld = ldc; return (char*)C + (i0 + j0 * ldc) * es; }
+        if (dC || direct_c) { cld = ldc; return (char*)C + (i0 + j0 * ldc) * es; }
         const int64_t t = step / ntk;
         int64_t mi = std::min(tm, m - i0);
         cld = mi;
@@ -269,7 +276,7 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
         const int r = (int)(step % R);
         const int64_t t = step / ntk, kt = step % ntk;
         const int c = (int)(t % R);
-        if (kt == 0 && !dC && !beta_zero) {  // C tile comes in once, before its first K slab
+        if (kt == 0 && !dC && !direct_c && !beta_zero) {  // C tile comes in once, before its first K slab
             if (cslot_used[c]) CGB_CUDA(cudaStreamWaitEvent(hs, ev_cout[c], 0));
             CGB_CHECK(copy2d(h->bufC[c].ptr, mi, (const char*)C + (i0 + j0 * ldc) * es, ldc, mi, nj, es,
                              cudaMemcpyHostToDevice, hs));
@@ -304,7 +311,7 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
         const int c = (int)(t % R);
         int64_t cld;
         char* cdev = cdev_of(step, i0, j0, cld);
-        if (kt == 0 && !dC) {
+        if (kt == 0 && !dC && !direct_c) {
             if (!beta_zero) CGB_CUDA(cudaStreamWaitEvent(cs, ev_cin[c], 0));
             else if (cslot_used[c]) CGB_CUDA(cudaStreamWaitEvent(cs, ev_cout[c], 0));  // slot drained before overwrite
         }
@@ -327,7 +334,8 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
             if (ti_info.slices) *info = ti_info;
             CGB_CUDA(cudaEventRecord(ev_free[r], cs));
         }
-        if (kt == ntk - 1 && !dC) {  // tile final: drain it on the D2H stream
+        if (kt == ntk - 1 && direct_c) h->last_d2h_bytes += mi * nj * es;  // written in place by the GEMM
+        if (kt == ntk - 1 && !dC && !direct_c) {  // tile final: drain it on the D2H stream
             CGB_CUDA(cudaEventRecord(ev_cdone[c], cs));
             CGB_CUDA(cudaStreamWaitEvent(ds, ev_cdone[c], 0));
             if (keep_on_device) {

@@ -329,7 +329,16 @@ typedef struct cosma_gpu_grouped_info {
  * data present at creation and re-checked on the device at every run; a
  * problem whose data then needs more slices, or holds Inf/NaN, is left to the
  * single-problem path.  Runs of an Ozaki plan synchronise `stream` (the host
- * reads the check), and tuning (tile order) runs only for beta == 0 batches. */
+ * reads the check), and tuning (tile order) runs only for beta == 0 batches.
+ *
+ * method COSMA_GPU_METHOD_OZAKI2 gives the Chinese-remainder form: one
+ * modulus count N for the batch (the most any problem's data needs, from the
+ * same rule as cosma_gpu_dgemm_ozaki2_device), each problem's fraction bits
+ * the most N admits at its k; the graph scales, splits into residues,
+ * multiplies every 128 x 128 tile's N modular products on the BF16 tensor
+ * cores and reconstructs each entry with one rounding.  The same re-check
+ * and single-problem fall-back apply; problems with k > 65536 always take
+ * the single-problem path. */
 typedef struct cosma_gpu_grouped_plan cosma_gpu_grouped_plan;
 cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count,
                                                       const cosma_gpu_gemm_problem* problems,
@@ -337,8 +346,9 @@ cosma_gpu_grouped_plan* cosma_gpu_grouped_plan_create(int method, int count,
 /* Replays the plan's CUDA graph on `stream` (asynchronous for native plans). */
 int cosma_gpu_grouped_plan_run(cosma_gpu_grouped_plan* plan, void* stream);
 int cosma_gpu_grouped_plan_info(cosma_gpu_grouped_plan* plan, cosma_gpu_grouped_info* info);
-/* Slice count planned for each problem of an Ozaki plan (`count` ints; 0 for
- * problems the plan does not slice, and for every problem of a native plan). */
+/* Slice count planned for each problem of an Ozaki plan, or the modulus count
+ * of the batch for each problem of a Chinese-remainder plan (`count` ints; 0
+ * for problems the plan does not take, and for every problem of a native plan). */
 int cosma_gpu_grouped_plan_slices(cosma_gpu_grouped_plan* plan, int* slices);
 void cosma_gpu_grouped_plan_destroy(cosma_gpu_grouped_plan* plan);
 /* One-shot grouped GEMM (plan without tuning, run, synchronise, destroy). */

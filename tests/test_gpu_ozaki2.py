@@ -219,3 +219,37 @@ def test_full_result_accuracy_at_4096(native_lib, cuda):
     normwise = dE.abs() / absab
     assert float(normwise.max()) <= 2.0 ** -52, info
     assert float(rel.max()) <= 1e-15, (float(rel.max()), int((rel > 1e-15).sum()), info)
+
+
+@pytest.mark.parametrize("scalar", ["d", "z"])
+def test_tiled_mm_one_step_c_in_place(native_lib, cuda, monkeypatch, scalar):
+    """A one-step Tiled-MM call with the Chinese-remainder method: the
+    reconstruction kernel reads and writes host C in place (device access to
+    host memory) or C is staged through a device slot; both give the bits of
+    the device-pointer call, and the D2H count still reports C once."""
+    from cosma_gb300 import dgemm_ozaki2_device, gemm, make_context, zgemm_ozaki2_device
+    dt = np.float64 if scalar == "d" else np.complex128
+    m, n, k = 150, 97, 210
+    ldc = m + 3
+    A = oracle.uniform((m, k), 61, dtype=dt)
+    B = oracle.uniform((n, k), 62, dtype=dt)
+    C0 = np.asfortranarray(oracle.uniform((ldc, n), 63, dtype=dt))
+    alpha, beta = (0.75, -0.5) if scalar == "d" else (0.75 - 0.25j, 0.5 + 1j)
+    tb = "T" if scalar == "d" else "C"
+    outs = []
+    for direct in ("ON", "OFF"):
+        monkeypatch.setenv("COSMA_GPU_HOST_DIRECT", direct)
+        h = make_context(scalar, 2)
+        h.set_method("ozaki2", 20)
+        Cg = C0.copy(order="F")
+        gemm(h, "N", tb, m, n, k, alpha, A, m, B, n, beta, Cg, ldc)
+        assert h.transfer_bytes()[1] == m * n * Cg.itemsize
+        h.close()
+        outs.append(Cg)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C0[:m], ldc)
+    run = dgemm_ozaki2_device if scalar == "d" else zgemm_ozaki2_device
+    run("N", tb, m, n, k, alpha, dA, m, dB, n, beta, dC, ldc, moduli=20)
+    want = from_dev(dC, m, n, ldc)
+    for got in outs:
+        np.testing.assert_array_equal(got[:m], want)
+        np.testing.assert_array_equal(got[m:], C0[m:])  # rows past m untouched
