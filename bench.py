@@ -44,11 +44,11 @@ UNIT = "TFLOP/s"
 # kernels of one headline step: A exponents (partial + combine), B exponents,
 # A residues, B residues, modular GEMM, reconstruction
 KERNELS_PER_STEP = 7
-# DRAM bytes (read + write) of one launch of the modular GEMM kernel at
-# m = n = k = 8192 with 18 moduli, from an ncu capture of that launch; DRAM
-# traffic of the kernel grows with its flops (a fixed wave footprint streams
-# each operand panel once per wave), so a 16384^3 launch moves 8x as much.
-TRAFFIC_BYTES_8192 = None
+# DRAM bytes of one launch of the modular GEMM kernel on the headline
+# workload itself (m = n = k = 16384, u*2^e inputs with phi = 0, 16 moduli):
+# dram__bytes_read.sum + dram__bytes_write.sum from a one-pass ncu capture
+# of that launch (the command is in profiles/ozaki2_gemm_pair_16384_dram.md)
+TRAFFIC_BYTES_16384 = {16: 137_887_403_520 + 4_843_662_848}
 CONFIG_NAMES = ("plain", "pdgemm", "grouped", "sgemm", "stream")
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no FP64 figure is measured on this machine)
 
@@ -67,9 +67,10 @@ def parse():
     p.add_argument("--no-configs", action="store_true", help="headline line only")
     p.add_argument("--count", type=int, default=10000,
                    help="problems in the grouped configuration (10,000; fewer for profiler captures)")
-    p.add_argument("--config", default="precision", choices=("precision",) + CONFIG_NAMES,
+    p.add_argument("--config", default="precision", choices=("precision",) + CONFIG_NAMES + ("grouped_crt",),
                    help="precision: the headline line (with the other configurations under 'configs'); "
-                        "otherwise one configuration alone")
+                        "otherwise one configuration alone (grouped_crt: the grouped batch in the "
+                        "Chinese-remainder form only, for profiler captures)")
     return p.parse_args()
 
 
@@ -438,18 +439,13 @@ def cfg_sgemm(steps, warmup, n=16384):
             "clocks": clocks, "gpu_launches": 3 * steps}
 
 
-def cfg_grouped(steps, warmup, count=10000):
-    """10,000 independent FP64 GEMMs, m, n, k log-uniform integers in [16, 1024],
-    transa/transb uniform in {N, T}, U[-1, 1] entries: one persistent grouped
-    launch (autotuned, CUDA graph) in native FP64 and in the digit-slice Ozaki
-    form and in the Chinese-remainder form, against a loop of per-problem
-    drop-in calls."""
+def grouped_batch(count, dev):
+    """The batching configuration's batch on `dev`: m, n, k log-uniform integers
+    in [16, 1024] (seed 2024), transa / transb uniform in {N, T}, U[-1, 1]
+    entries (torch generator seed 7), alpha = 1, beta = 0, packed one after
+    another (32-element aligned) in three device arrays."""
     import torch
 
-    import cosma_gb300 as cg
-    import oracle
-
-    dev = torch.device("cuda", 0)
     rng = np.random.default_rng(2024)
     draw = lambda: np.clip(np.round(np.exp(rng.uniform(np.log(16), np.log(1024), count))), 16, 1024).astype(np.int64)
     m, n, k = draw(), draw(), draw()
@@ -469,6 +465,47 @@ def cfg_grouped(steps, warmup, count=10000):
         ldb = int(k[i] if tb[i] == "N" else n[i])
         probs.append((str(ta[i]), str(tb[i]), int(m[i]), int(n[i]), int(k[i]), 1.0, pa + 8 * int(sa[i]), lda,
                       pb + 8 * int(sb[i]), ldb, 0.0, pc + 8 * int(sc[i]), int(m[i])))
+    return rng, (m, n, k, ta, tb), (sa, sb, sc), (dA, dB, dC), probs
+
+
+def cfg_grouped_crt(steps, warmup, count=10000):
+    """The batching configuration's batch in the Chinese-remainder form alone
+    (plan, warm-up runs, timed runs): the command behind the grouped launch
+    lists and kernel captures."""
+    import torch
+
+    import cosma_gb300 as cg
+
+    dev = torch.device("cuda", 0)
+    _, (m, n, k, _, _), _, bufs, probs = grouped_batch(count, dev)
+    useful = float((2 * m * n * k).sum())
+    s = torch.cuda.current_stream(dev)
+    plan = cg.GroupedPlan(probs, method="ozaki2", autotune=False)
+    for _ in range(warmup):
+        plan.run(stream=s)
+    ms, _ = cuda_ms(lambda: plan.run(stream=s), s, max(steps, 1))
+    info = plan.info()
+    plan.close()
+    return {"metric": f"grouped FP64-accurate GEMM TFLOP/s ({count:,} uneven problems, Chinese-remainder form)",
+            "value": useful / (ms * 1e-3) / 1e12, "unit": UNIT, "steps": steps, "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic U[-1,1], seeded",
+            "config": {"workload": f"batching: {count:,} FP64 GEMMs, m,n,k log-uniform in [16,1024], random N/T"},
+            "plan": info}
+
+
+def cfg_grouped(steps, warmup, count=10000):
+    """10,000 independent FP64 GEMMs, m, n, k log-uniform integers in [16, 1024],
+    transa/transb uniform in {N, T}, U[-1, 1] entries: one persistent grouped
+    launch (autotuned, CUDA graph) in native FP64 and in the digit-slice Ozaki
+    form and in the Chinese-remainder form, against a loop of per-problem
+    drop-in calls."""
+    import torch
+
+    import cosma_gb300 as cg
+    import oracle
+
+    dev = torch.device("cuda", 0)
+    rng, (m, n, k, ta, tb), (sa, sb, sc), (dA, dB, dC), probs = grouped_batch(count, dev)
     useful = float((2 * m * n * k).sum())
     s = torch.cuda.current_stream(dev)
 
@@ -823,7 +860,7 @@ def cfg_stream(steps, warmup, n=16384, tile=8192):
 
 
 CONFIGS = {"plain": cfg_plain, "pdgemm": cfg_pdgemm, "grouped": cfg_grouped, "sgemm": cfg_sgemm,
-           "stream": cfg_stream}
+           "stream": cfg_stream, "grouped_crt": cfg_grouped_crt}
 
 
 # ----------------------------------------------------------------- headline
@@ -965,10 +1002,12 @@ def headline(args):
     achieved = info["slices"] * flops / (kms * 1e-3) / 1e12
     peak = pk["bf16_tflops_sustained"]
     traffic = None
-    if TRAFFIC_BYTES_8192 is not None and n == 16384:
-        traffic = {"bytes": int(TRAFFIC_BYTES_8192 * 8),
-                   "scaled_from": "ncu capture of one launch at m=n=k=8192 (dram__bytes_read.sum + "
-                                  "dram__bytes_write.sum) x 8 (the flops ratio)"}
+    if n == 16384 and args.phi == 0 and info["slices"] in TRAFFIC_BYTES_16384:
+        traffic = {"bytes": TRAFFIC_BYTES_16384[info["slices"]],
+                   "scaled_from": "one-pass ncu capture of this launch on this workload (dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum); algorithmic: residues read once "
+                                  f"{2 * info['slices'] * n * n * 2 / 1e9:.1f} GB, residue bytes written "
+                                  f"{info['slices'] * n * n / 1e9:.1f} GB"}
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "frac_of_burst": achieved / pk["bf16_tflops"], "traffic": traffic["bytes"] if traffic else None,
                 "traffic_note": traffic["scaled_from"] if traffic else None,
@@ -1016,7 +1055,10 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.config != "precision":
-        out = CONFIGS[args.config](args.steps, args.warmup)
+        if args.config in ("grouped", "grouped_crt"):
+            out = CONFIGS[args.config](args.steps, args.warmup, count=args.count)
+        else:
+            out = CONFIGS[args.config](args.steps, args.warmup)
         out.update({"n_gpus": 1, "warmup": max(args.warmup, 3), "scaling": "weak", "vs_baseline": None})
         print(json.dumps(out), flush=True)
         return

@@ -107,6 +107,7 @@ SIGNATURES = {
     "cosma_gpu_dgemm_ozaki2_residual": (i32, [ch, ch, i64, i64, i64, vp, i64, vp, i64, vp, i64, i32, vp, vp, i64, vp,
                                               C.POINTER(OzakiInfo)]),
     "cosma_gpu_ozaki2_choose": (i32, [i64, dbl, i32, i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "cosma_gpu_release_workspaces": (i32, [vp]),
     "cosma_gpu_dgemm_ozaki_noalloc": (i32, [ch, ch, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64, i32, vp,
                                             C.POINTER(OzakiInfo)]),
     "cosma_gpu_grouped_plan_create": (vp, [i32, i32, C.POINTER(GemmProblem), i32, vp]),

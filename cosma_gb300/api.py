@@ -281,6 +281,12 @@ def dgemm_ozaki2_residual(transa, transb, m, n, k, A, lda, B, ldb, Ct, ldt, E, R
     return info.as_dict()
 
 
+def release_workspaces(stream=None):
+    """Frees the precision forms' workspaces kept for `stream` (call before
+    the stream is destroyed; its work must be complete)."""
+    N.check(N.load().cosma_gpu_release_workspaces(_stream_ptr(stream)))
+
+
 def ozaki2_choose(k, spread_bits=0.0, moduli=0, exact_bits=0):
     """(modulus count, fraction bits P) the Chinese-remainder form uses (host only)."""
     lib = N.load()

@@ -132,6 +132,13 @@ int cosma_gpu_dgemm_ozaki_device(char ta, char tb, int64_t m, int64_t n, int64_t
     return cgb::gemm_device(g, COSMA_GPU_METHOD_OZAKI, slices, (cudaStream_t)stream, info);
 }
 
+int cosma_gpu_release_workspaces(void* stream) {
+    cgb::clear_error();
+    cgb::ozaki_release_stream((cudaStream_t)stream);
+    cgb::ozaki2_release_stream((cudaStream_t)stream);
+    return COSMA_GPU_SUCCESS;
+}
+
 int cosma_gpu_dgemm_ozaki2_device(char ta, char tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
                                   int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
                                   int moduli, void* stream, cosma_gpu_ozaki_info* info) {

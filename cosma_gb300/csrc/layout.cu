@@ -126,16 +126,20 @@ template <> __device__ __forceinline__ float sub_rn(float a, float b) { return _
 // instead of an FP64 multiply (GB300's FP64 pipe, not HBM, bounds the
 // unpack otherwise); zeros, subnormals, Inf/NaN and results that leave the
 // normal range take the multiply, so the result is fl(s*x) bit for bit.
+// The rare multiply is a call, so that the compiler branches around it
+// instead of issuing it predicated on every element.
+__device__ __noinline__ double mul_rare(double s, double x) { return __dmul_rn(s, x); }
+__device__ __noinline__ float mul_rare(float s, float x) { return __fmul_rn(s, x); }
 __device__ __forceinline__ double mul_pow2(double s, int e, double x) {
     const long long b = __double_as_longlong(x);
     const int ex = (int)((b >> 52) & 0x7FF), ne = ex + e;
-    if (ex == 0 || ex == 0x7FF || ne <= 0 || ne >= 0x7FF) return __dmul_rn(s, x);
+    if (ex == 0 || ex == 0x7FF || ne <= 0 || ne >= 0x7FF) return mul_rare(s, x);
     return __longlong_as_double(b + ((long long)e << 52));
 }
 __device__ __forceinline__ float mul_pow2(float s, int e, float x) {
     const int b = __float_as_int(x);
     const int ex = (b >> 23) & 0xFF, ne = ex + e;
-    if (ex == 0 || ex == 0xFF || ne <= 0 || ne >= 0xFF) return __fmul_rn(s, x);
+    if (ex == 0 || ex == 0xFF || ne <= 0 || ne >= 0xFF) return mul_rare(s, x);
     return __int_as_float(b + (e << 23));
 }
 
@@ -153,11 +157,11 @@ __host__ ScaleMode<R> scale_mode(double s) {
     if (f == 0.5 && std::isfinite(s)) return {1, e - 1};
     return {2, 0};
 }
-template <class R>
-__device__ __forceinline__ R apply_scale(const ScaleMode<R>& m, R s, R x) {
-    if (m.mode == 0) return x;
-    if (m.mode == 1) return mul_pow2(s, m.e, x);
-    return mul_rn(s, x);
+template <int MODE, class R>
+__device__ __forceinline__ R apply_scale(R s, int e, R x) {
+    if constexpr (MODE == 0) return x;
+    else if constexpr (MODE == 1) return mul_pow2(s, e, x);
+    else return mul_rn(s, x);
 }
 
 // real: d = fl(fl(alpha*s) + fl(beta*d)); beta == 0 -> d = fl(alpha*s).  The
@@ -169,11 +173,12 @@ __device__ __forceinline__ R apply_scale(const ScaleMode<R>& m, R s, R x) {
 // issues all their loads before any arithmetic: GB300's FP64 pipe is narrow
 // (the multiply and add of one element cost about what its 24 bytes of HBM
 // traffic do), so the loads of the next elements must be in flight while the
-// FP64 work of the current ones runs.
-template <class R>
-__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, ScaleMode<R> am, const R* __restrict__ src,
-                                   int64_t lds, R beta, ScaleMode<R> bm, R* __restrict__ dst, int64_t ldd,
-                                   int read_dst) {
+// FP64 work of the current ones runs.  The modes are template parameters:
+// with runtime modes the compiler issues every mode's FP64 multiply,
+// predicated, for every element.
+template <class R, int AM, int BM, bool READ>
+__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, int ae, const R* __restrict__ src,
+                                   int64_t lds, R beta, int be, R* __restrict__ dst, int64_t ldd) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t j = blockIdx.y; j < cols; j += gridDim.y) {
         const R* s = src + j * lds;
@@ -184,14 +189,14 @@ __global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, ScaleMod
             for (int q = 0; q < 4; ++q) {
                 const int64_t i = i0 + q * stride;
                 x[q] = i < rows ? s[i] : R(0);
-                y[q] = (read_dst && i < rows) ? d[i] : R(0);
+                y[q] = (READ && i < rows) ? d[i] : R(0);
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int64_t i = i0 + q * stride;
                 if (i >= rows) break;
-                R v = apply_scale(am, alpha, x[q]);
-                if (read_dst) v = add_rn(v, apply_scale(bm, beta, y[q]));
+                R v = apply_scale<AM>(alpha, ae, x[q]);
+                if constexpr (READ) v = add_rn(v, apply_scale<BM>(beta, be, y[q]));
                 d[i] = v;
             }
         }
@@ -296,6 +301,25 @@ int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t c
     return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "pack: elem_bytes must be 4, 8 or 16");
 }
 
+// The real unpack for the scale modes of alpha and beta (beta's only when C
+// is read).
+template <class R>
+void launch_unpack_real(dim3 g, cudaStream_t st, int64_t rows, int64_t cols, R alpha, ScaleMode<R> am, const R* src,
+                        int64_t lds, R beta, ScaleMode<R> bm, R* dst, int64_t ldd, bool read_dst) {
+#define CGB_UNPACK(A, B, RD) \
+    unpack_real_kernel<R, A, B, RD><<<g, 256, 0, st>>>(rows, cols, alpha, am.e, src, lds, beta, bm.e, dst, ldd)
+#define CGB_UNPACK_B(A)                              \
+    if (!read_dst) CGB_UNPACK(A, 0, false);          \
+    else if (bm.mode == 0) CGB_UNPACK(A, 0, true);   \
+    else if (bm.mode == 1) CGB_UNPACK(A, 1, true);   \
+    else CGB_UNPACK(A, 2, true);
+    if (am.mode == 0) { CGB_UNPACK_B(0) }
+    else if (am.mode == 1) { CGB_UNPACK_B(1) }
+    else { CGB_UNPACK_B(2) }
+#undef CGB_UNPACK_B
+#undef CGB_UNPACK
+}
+
 int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, const void* src, int64_t lds,
                   const double* beta, void* dst, int64_t ldd, cudaStream_t s) {
     if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
@@ -307,14 +331,13 @@ int unpack_device(Scalar sc, int64_t rows, int64_t cols, const double* alpha, co
     dim3 g4 = grid2d(ceil_div(rows, 4), cols, 256);  // the real kernels take four elements per thread
     switch (sc) {
         case Scalar::D:
-            unpack_real_kernel<double><<<g4, 256, 0, s>>>(rows, cols, alpha[0], scale_mode<double>(alpha[0]),
-                                                         (const double*)src, lds, beta[0], scale_mode<double>(beta[0]),
-                                                         (double*)dst, ldd, read_dst);
+            launch_unpack_real<double>(g4, s, rows, cols, alpha[0], scale_mode<double>(alpha[0]), (const double*)src,
+                                       lds, beta[0], scale_mode<double>(beta[0]), (double*)dst, ldd, read_dst);
             break;
         case Scalar::S:
-            unpack_real_kernel<float><<<g4, 256, 0, s>>>(rows, cols, (float)alpha[0], scale_mode<float>((float)alpha[0]),
-                                                        (const float*)src, lds, (float)beta[0],
-                                                        scale_mode<float>((float)beta[0]), (float*)dst, ldd, read_dst);
+            launch_unpack_real<float>(g4, s, rows, cols, (float)alpha[0], scale_mode<float>((float)alpha[0]),
+                                      (const float*)src, lds, (float)beta[0], scale_mode<float>((float)beta[0]),
+                                      (float*)dst, ldd, read_dst);
             break;
         case Scalar::Z:
             unpack_cplx_kernel<double, double2><<<g, 256, 0, s>>>(rows, cols, alpha[0], alpha[1],

@@ -578,6 +578,28 @@ Workspace* workspace(cudaStream_t s) {
     return w;
 }
 
+// Frees the workspace of a stream that is about to be destroyed: a later
+// stream may get the same handle and must not inherit it (nor may the memory
+// outlive the stream).  Work on the stream must be complete.
+void release_workspace(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    Workspace* w = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_ws_mu);
+        auto it = g_ws.find({dev, s});
+        if (it == g_ws.end()) return;
+        w = it->second;
+        g_ws.erase(it);
+    }
+    if (w->host_stats) cudaFreeHost(w->host_stats);
+    if (w->host_err) cudaFreeHost(w->host_err);
+    for (auto e : w->ev)
+        if (e) cudaEventDestroy(e);
+    delete w;  // the device buffers free themselves
+    cudaGetLastError();
+}
+
 int num_sms() { return device_sm_count(); }
 
 // Slice count from the requested accuracy and the measured exponent spread.
@@ -1026,6 +1048,8 @@ int ozaki_zchunk(const GemmDesc& g, int slices, cudaStream_t st, cosma_gpu_ozaki
 }
 
 }  // namespace oz
+
+void ozaki_release_stream(cudaStream_t s) { oz::release_workspace(s); }
 
 int ozaki_dgemm(const GemmDesc& g, int slices, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
     if (g.scalar != Scalar::D) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki: double only");

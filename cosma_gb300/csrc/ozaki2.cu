@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
             double x = 0.0;
             if (r < rows && l < k) x = Xd[2 * (KCONTIG ? l + r * ld : r + l * ld) + part];
             v[e] = scaled_integer(x, E, sp.P);
-            if (part && conj) v[e].sgn = -v[e].sgn;  // the conjugated imaginary part
+            if (part && conj) v[e].sgn ^= 0x80000000u;  // the conjugated imaginary part
         }
 #pragma unroll 1
         for (int m = 0; m < sp.nmod; ++m) {
@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
                 w[e / 2] = pack_bf16(residue_bits<NL>(v[e], p, mg, h, bias, sp.c13[m]),
-                                     residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m]));
+                                     residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m])) ^
+                           pair_signs(v[e], v[e + 1]);
                 nw[e / 2] = w[e / 2] ^ 0x80008000u;  // the negated pair: both sign bits flipped
             }
             uint16_t* base = out + m * slab;
@@ -367,8 +368,16 @@ struct CombineParams {
 // GEMM columns (block b: row block b % row_blocks, column block b /
 // row_blocks); warp g takes columns 16 cb + 4 g .. + 3, lane the row 32 rb +
 // lane, and one 32-bit load gives the thread its four residues of a modulus.
-template <int L, bool RESIDUAL>
+// MODE: kStoreC writes the rounded product, kScaleC alpha * it + beta * C,
+// kResidual the residual pair.  The store-only form is its own instantiation:
+// the compiler predicates rather than branches around the alpha / beta
+// arithmetic, and three predicated FP64 instructions per entry occupy
+// GB300's narrow FP64 pipe.
+constexpr int kStoreC = 0, kScaleC = 1, kResidual = 2;
+
+template <int L, int MODE>
 __global__ void __launch_bounds__(128) combine_kernel(const __grid_constant__ CombineParams p) {
+    constexpr bool RESIDUAL = MODE == kResidual;
     const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
     const int64_t rb = (int64_t)blockIdx.x % p.row_blocks, cb = (int64_t)blockIdx.x / p.row_blocks;
     const int64_t i = rb * 32 + lane;
@@ -384,20 +393,7 @@ __global__ void __launch_bounds__(128) combine_kernel(const __grid_constant__ Co
     const uint32_t* rp = reinterpret_cast<const uint32_t*>(p.R + (cb * p.m_pad + i) * 16) + g;
     const int64_t stride = p.nb16 * p.m_pad * 4;  // 32-bit words per modulus
     unsigned long long acc[4][L];
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int l = 0; l < L; ++l) acc[c][l] = 0;
-#pragma unroll 2
-    for (int t = 0; t < p.nmod; ++t) {
-        const uint32_t r4 = __ldg(rp + t * stride);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t r = (r4 >> (8 * c)) & 0xFFu;
-#pragma unroll
-            for (int l = 0; l < L; ++l) acc[c][l] += (unsigned long long)r * p.crt.w[t][l];
-        }
-    }
+    crt_accumulate<L>(rp, stride, p.nmod, p.crt, acc);
     const int Ei = p.expA[i];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -438,8 +434,10 @@ __global__ void __launch_bounds__(128) combine_kernel(const __grid_constant__ Co
             continue;
         }
         double* cp = p.C + (i + j * p.ldc) * p.cs + part;
-        if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
-        if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+        if constexpr (MODE == kScaleC) {
+            if (!p.alpha_one) r = __dmul_rn(p.alpha, r);
+            if (!p.beta_zero) r = __dadd_rn(r, __dmul_rn(p.beta, *cp));
+        }
         *cp = r;
     }
 }
@@ -658,6 +656,28 @@ Workspace* workspace(cudaStream_t s) {
     return w;
 }
 
+// Frees the workspace of a stream that is about to be destroyed: a later
+// stream may get the same handle and must not inherit it (nor may the memory
+// outlive the stream).  Work on the stream must be complete.
+void release_workspace(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    Workspace* w = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_ws_mu);
+        auto it = g_ws.find({dev, s});
+        if (it == g_ws.end()) return;
+        w = it->second;
+        g_ws.erase(it);
+    }
+    if (w->host_stats) cudaFreeHost(w->host_stats);
+    if (w->host_err) cudaFreeHost(w->host_err);
+    for (auto e : w->ev)
+        if (e) cudaEventDestroy(e);
+    delete w;  // the device buffers free themselves
+    cudaGetLastError();
+}
+
 int pair_grid(int units, int* grid) {
     static PerDevice<int> pairs;
     int n = 0;
@@ -709,14 +729,14 @@ int launch_gemm(const void* resA, const void* resB, int64_t k_pad, const GemmPar
     return COSMA_GPU_SUCCESS;
 }
 
-template <bool RESIDUAL>
+template <int MODE>
 void launch_combine_t(const CombineParams& cp, int limbs, unsigned grid, cudaStream_t st) {
     switch (limbs) {
-        case 4: combine_kernel<4, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
-        case 5: combine_kernel<5, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
-        case 6: combine_kernel<6, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
-        case 7: combine_kernel<7, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
-        default: combine_kernel<8, RESIDUAL><<<grid, 128, 0, st>>>(cp); break;
+        case 4: combine_kernel<4, MODE><<<grid, 128, 0, st>>>(cp); break;
+        case 5: combine_kernel<5, MODE><<<grid, 128, 0, st>>>(cp); break;
+        case 6: combine_kernel<6, MODE><<<grid, 128, 0, st>>>(cp); break;
+        case 7: combine_kernel<7, MODE><<<grid, 128, 0, st>>>(cp); break;
+        default: combine_kernel<8, MODE><<<grid, 128, 0, st>>>(cp); break;
     }
 }
 
@@ -724,8 +744,10 @@ int launch_combine(CombineParams& cp, int nmod, int64_t gemm_cols, cudaStream_t 
     cp.row_blocks = ceil_div(cp.m, 32);
     const int64_t blocks = cp.row_blocks * ceil_div(gemm_cols, 16);
     if (blocks > 0x7FFFFFFF) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: C too large for the combine grid");
-    if (cp.E) launch_combine_t<true>(cp, limbs_for(nmod), (unsigned)blocks, st);
-    else launch_combine_t<false>(cp, limbs_for(nmod), (unsigned)blocks, st);
+    const int L = limbs_for(nmod);
+    if (cp.E) launch_combine_t<kResidual>(cp, L, (unsigned)blocks, st);
+    else if (cp.alpha_one && cp.beta_zero) launch_combine_t<kStoreC>(cp, L, (unsigned)blocks, st);
+    else launch_combine_t<kScaleC>(cp, L, (unsigned)blocks, st);
     CGB_CUDA(cudaGetLastError());
     return COSMA_GPU_SUCCESS;
 }
@@ -1017,6 +1039,8 @@ extern "C" int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int exact_
 }
 
 namespace cgb {
+
+void ozaki2_release_stream(cudaStream_t s) { oz2::release_workspace(s); }
 
 int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
     if (g.scalar != Scalar::D) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: double only");

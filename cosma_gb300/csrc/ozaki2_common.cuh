@@ -41,17 +41,18 @@ struct SplitParams {
 };
 
 // The scaled integer X = round_half_away(|x| 2^(P - E)) of one operand
-// element as 13-bit limbs (X < 2^(P+1)), with its sign as +-1.0f.  |x| = M
-// 2^eu with the 53-bit significand M; X = M 2^sh exactly when sh >= 0.
+// element as 13-bit limbs (X < 2^(P+1)), with its sign as an FP32 sign bit
+// (0x80000000 for negative x).  |x| = M 2^eu with the 53-bit significand M;
+// X = M 2^sh exactly when sh >= 0.
 struct Scaled {
     uint32_t d[LIMB13];
-    float sgn;
+    uint32_t sgn;
 };
 
 __device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     Scaled v;
-    v.sgn = (b >> 63) ? -1.0f : 1.0f;
+    v.sgn = (uint32_t)(b >> 32) & 0x80000000u;
     const int ef = (int)((b >> 52) & 0x7FF);
     unsigned long long M = b & 0xFFFFFFFFFFFFFull;
     int eu;
@@ -80,14 +81,15 @@ __device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
     return v;
 }
 
-// FP32 bits of the balanced residue of the signed scaled integer modulo p,
-// b = ((X + h) mod p) - h in [-h, p - 1 - h] (|b| <= 127), sign applied.
+// FP32 bits of the balanced residue of the magnitude X modulo p,
+// b = ((X + h) mod p) - h in [-h, p - 1 - h] (|b| <= 127); the residue of the
+// signed integer is -b for negative x (the caller flips the sign bit).
 // u = X_0 + h + sum_i X_i (2^(13 i) mod p) stays below 2^24 (NL <= 9), where
 // umulhi(u, ceil(2^32 / p)) is exactly floor(u / p) for every modulus here
 // (checked exhaustively), so r = u - q p needs no correction.  The value is
 // then formed on the FP32 pipe: 2^23 + r has the bits 0x4B000000 | r, and
-// (2^23 + r - 2^23 - h) * sign is exact.  Its upper 16 bits are its BF16
-// encoding (exact: at most 8 significant bits).
+// 2^23 + r - 2^23 - h is exact.  Its upper 16 bits are its BF16 encoding
+// (exact: at most 8 significant bits).
 template <int NL>
 __device__ __forceinline__ uint32_t residue_bits(const Scaled& v, uint32_t p, uint32_t magic, uint32_t h, float bias,
                                                  const uint32_t* c13) {
@@ -95,12 +97,15 @@ __device__ __forceinline__ uint32_t residue_bits(const Scaled& v, uint32_t p, ui
 #pragma unroll
     for (int i = 1; i < NL; ++i) u += v.d[i] * c13[i];
     const uint32_t r = u - __umulhi(u, magic) * p;
-    const float f = (__uint_as_float(0x4B000000u | r) + bias) * v.sgn;
-    return __float_as_uint(f);
+    return __float_as_uint(__uint_as_float(0x4B000000u | r) + bias);
 }
 
 // Two FP32 residues packed as two BF16 values (upper halves), low one first.
 __device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) { return __byte_perm(lo, hi, 0x7632); }
+
+// The sign bits of a packed BF16 pair of residues of (lo, hi): XOR-ed into
+// the pair, they give the residues of the signed integers.
+__device__ __forceinline__ uint32_t pair_signs(const Scaled& lo, const Scaled& hi) { return (lo.sgn >> 16) | hi.sgn; }
 
 // Residues of one block of 32 rows x 64 K elements of a real (rows x k)
 // operand into N BF16 matrices [t][rows_pad][k_pad], zero padded; 256
@@ -129,6 +134,9 @@ __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_
     }
     uint16_t* o = out + r * k_pad + l0;
     const int64_t slab = rows_pad * k_pad;
+    uint32_t sg[4];
+#pragma unroll
+    for (int e = 0; e < 8; e += 2) sg[e / 2] = pair_signs(v[e], v[e + 1]);
 #pragma unroll 1
     for (int m = 0; m < sp.nmod; ++m) {
         const uint32_t p = sp.p[m], mg = sp.magic[m], h = sp.h[m];
@@ -137,7 +145,7 @@ __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_
 #pragma unroll
         for (int e = 0; e < 8; e += 2)
             w[e / 2] = pack_bf16(residue_bits<NL>(v[e], p, mg, h, bias, sp.c13[m]),
-                                 residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m]));
+                                 residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m])) ^ sg[e / 2];
         *reinterpret_cast<uint4*>(o + m * slab) = make_uint4(w[0], w[1], w[2], w[3]);
     }
 }
@@ -152,9 +160,10 @@ struct CrtConst {
 };
 
 // Round-to-nearest-even conversion of the unsigned 128-bit integer (hi:lo)
-// times 2^e2 to double (subnormal and overflow results included).
-__device__ __forceinline__ double u128_to_double(unsigned long long lo, unsigned long long hi, int e2) {
-    if (hi == 0 && lo == 0) return 0.0;
+// times 2^e2 to the bits of a double (subnormal and overflow results
+// included), formed with integer operations only.
+__device__ __forceinline__ unsigned long long u128_to_bits(unsigned long long lo, unsigned long long hi, int e2) {
+    if (hi == 0 && lo == 0) return 0ull;
     const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
     int e_lsb = msb - 52 + e2;  // weight of the last kept bit for a normal result
     int r = msb - 52;           // bits dropped
@@ -197,7 +206,7 @@ __device__ __forceinline__ double u128_to_double(unsigned long long lo, unsigned
     } else {
         bits = mant;  // subnormal (or the smallest normal reached by rounding)
     }
-    return __longlong_as_double((long long)bits);
+    return bits;
 }
 
 // |x| (L limbs) * 2^e2 rounded once to FP64, negated if neg: the top four
@@ -222,8 +231,8 @@ __device__ __forceinline__ double limbs_to_double(const uint32_t (&x)[L], bool n
     }
     const unsigned long long hi = ((unsigned long long)w3 << 32) | w2;
     const unsigned long long lo = ((unsigned long long)w1 << 32) | w0 | (sticky ? 1ull : 0ull);
-    const double r = u128_to_double(lo, hi, e2 + 32 * (tl - 3));
-    return neg ? -r : r;
+    const unsigned long long bits = u128_to_bits(lo, hi, e2 + 32 * (tl - 3));
+    return __longlong_as_double((long long)(bits | ((unsigned long long)neg << 63)));  // sign by bit, no FP64 op
 }
 
 // x = m << s as limbs (m < 2^53, s + 53 <= 32 L).
@@ -268,8 +277,7 @@ __device__ __forceinline__ void sub_limbs(uint32_t (&x)[L], const uint32_t (&y)[
 // X - q M lies in (-0.51 M, 0.51 M) and is V itself, as an L-limb two's
 // complement number.  Returns |V| in x and its sign.
 template <int L>
-__device__ __forceinline__ bool reduce_crt(const unsigned long long (&acc)[L], uint32_t (&x)[L],
-                                           const CrtConst& p) {
+__device__ __forceinline__ bool reduce_crt(const unsigned long long (&acc)[L], uint32_t (&x)[L], const CrtConst& p) {
     unsigned long long c = 0;
 #pragma unroll
     for (int l = 0; l < L; ++l) {
@@ -292,6 +300,36 @@ __device__ __forceinline__ bool reduce_crt(const unsigned long long (&acc)[L], u
     const bool neg = (x[L - 1] >> 31) != 0;
     if (neg) negate_limbs<L>(x);
     return neg;
+}
+
+// X_c = sum_t r_{t,c} w_t (L 64-bit partial limbs) for the four residue bytes
+// c of the words rp[t * stride], t < nmod.  The words of eight moduli are
+// loaded before their products are summed, so that eight loads are in
+// flight per thread.
+template <int L>
+__device__ __forceinline__ void crt_accumulate(const uint32_t* __restrict__ rp, int64_t stride, int nmod,
+                                               const CrtConst& crt, unsigned long long (&acc)[4][L]) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int l = 0; l < L; ++l) acc[c][l] = 0;
+#pragma unroll 1
+    for (int t0 = 0; t0 < nmod; t0 += 8) {
+        uint32_t rr[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) rr[u] = t0 + u < nmod ? __ldg(rp + (int64_t)(t0 + u) * stride) : 0u;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (t0 + u >= nmod) break;
+            const int t = t0 + u;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const uint32_t r = (rr[u] >> (8 * c)) & 0xFFu;
+#pragma unroll
+                for (int l = 0; l < L; ++l) acc[c][l] += (unsigned long long)r * crt.w[t][l];
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------- host side

@@ -408,7 +408,10 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 // thread as in ozaki2.cu's combine_kernel: warp g takes columns 16 cb + 4 g
 // .. + 3, lane the row 32 rb + lane, and one 32-bit load gives the thread its
 // four residues of a modulus.
-template <int L>
+// SCALE: some problem of the batch has alpha != 1 or beta != 0 (otherwise
+// the alpha / beta arithmetic is left out of the instantiation: predicated
+// FP64 instructions would occupy GB300's narrow FP64 pipe).
+template <int L, bool SCALE>
 __global__ void __launch_bounds__(128) gcombine_kernel(const Prob* __restrict__ P, const Item* __restrict__ items,
                                                        const int* __restrict__ ok,
                                                        const __grid_constant__ CrtConst crt) {
@@ -423,20 +426,7 @@ __global__ void __launch_bounds__(128) gcombine_kernel(const Prob* __restrict__ 
     const uint32_t* rp = reinterpret_cast<const uint32_t*>(p.R + ((int64_t)it.z * m_pad + i) * 16) + g;
     const int64_t stride = (int64_t)(p.n_pad / 16) * m_pad * 4;  // 32-bit words per modulus
     unsigned long long acc[4][L];
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int l = 0; l < L; ++l) acc[c][l] = 0;
-#pragma unroll 2
-    for (int t = 0; t < crt.nmod; ++t) {
-        const uint32_t r4 = __ldg(rp + t * stride);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t r = (r4 >> (8 * c)) & 0xFFu;
-#pragma unroll
-            for (int l = 0; l < L; ++l) acc[c][l] += (unsigned long long)r * crt.w[t][l];
-        }
-    }
+    crt_accumulate<L>(rp, stride, crt.nmod, crt, acc);
     const int Ei = p.expA[i];
     const int twoP = 2 * p.P;
     const double alpha = p.alpha, beta = p.beta;
@@ -449,8 +439,10 @@ __global__ void __launch_bounds__(128) gcombine_kernel(const Prob* __restrict__ 
         const bool neg = reduce_crt<L>(acc[c], x, crt);
         double r = limbs_to_double<L>(x, neg, Ei + p.expB[j] - twoP);
         double* cp = p.C + i + j * p.ldc;
-        if (!alpha_one) r = __dmul_rn(alpha, r);
-        if (!beta_zero) r = __dadd_rn(r, __dmul_rn(beta, *cp));
+        if constexpr (SCALE) {
+            if (!alpha_one) r = __dmul_rn(alpha, r);
+            if (!beta_zero) r = __dadd_rn(r, __dmul_rn(beta, *cp));
+        }
         *cp = r;
     }
 }
@@ -469,6 +461,7 @@ using cgb::oz2g::Prob;
 struct cosma_gpu_oz2_grouped_plan {
     int count = 0;
     int nmod = 0, limbs13 = 5, extra = 16;
+    bool scale = false;  // some grouped problem has alpha != 1 or beta != 0
     std::vector<Prob> hp;
     std::vector<cosma_gpu_gemm_problem> orig;  // for the host-side recomputation of skipped problems
     std::vector<int> host_side;                // k == 0 or alpha == 0: C <- beta*C on every run
@@ -512,18 +505,25 @@ void launch_gsplit(const Plan* pl, cudaStream_t st) {
     }
 }
 
+template <bool SCALE>
+void launch_gcombine_l(int limbs, unsigned g, const Prob* P, const Item* it, const int* ok, const CrtConst& crt,
+                       cudaStream_t st) {
+    switch (limbs) {
+        case 4: gcombine_kernel<4, SCALE><<<g, 128, 0, st>>>(P, it, ok, crt); break;
+        case 5: gcombine_kernel<5, SCALE><<<g, 128, 0, st>>>(P, it, ok, crt); break;
+        case 6: gcombine_kernel<6, SCALE><<<g, 128, 0, st>>>(P, it, ok, crt); break;
+        case 7: gcombine_kernel<7, SCALE><<<g, 128, 0, st>>>(P, it, ok, crt); break;
+        default: gcombine_kernel<8, SCALE><<<g, 128, 0, st>>>(P, it, ok, crt); break;
+    }
+}
+
 void launch_gcombine(const Plan* pl, cudaStream_t st) {
     const Prob* P = (const Prob*)pl->probs.ptr;
     const Item* it = (const Item*)pl->citems.ptr;
     const int* ok = (const int*)pl->ok.ptr;
     const unsigned g = (unsigned)pl->n_citems;
-    switch (limbs_for(pl->nmod)) {
-        case 4: gcombine_kernel<4><<<g, 128, 0, st>>>(P, it, ok, pl->crt); break;
-        case 5: gcombine_kernel<5><<<g, 128, 0, st>>>(P, it, ok, pl->crt); break;
-        case 6: gcombine_kernel<6><<<g, 128, 0, st>>>(P, it, ok, pl->crt); break;
-        case 7: gcombine_kernel<7><<<g, 128, 0, st>>>(P, it, ok, pl->crt); break;
-        default: gcombine_kernel<8><<<g, 128, 0, st>>>(P, it, ok, pl->crt); break;
-    }
+    if (pl->scale) launch_gcombine_l<true>(limbs_for(pl->nmod), g, P, it, ok, pl->crt, st);
+    else launch_gcombine_l<false>(limbs_for(pl->nmod), g, P, it, ok, pl->crt, st);
 }
 
 // All launches of one run, in stream order (captured into the plan's graph).
@@ -816,6 +816,7 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
         for (int cb = 0; cb < (int)ceil_div(p.n, 16); ++cb)
             for (int rb = 0; rb < (int)ceil_div(p.m, 32); ++rb) citems.push_back(make_int4(i, rb, cb, 0));
         pl->padded += 2.0 * nmod * (double)p.m_pad * p.n_pad * p.k_pad;
+        pl->scale |= !p.alpha_one || !p.beta_zero;
     }
     if (sitems.size() > 0x7FFFFFFFu || citems.size() > 0x7FFFFFFFu)
         return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "grouped ozaki2: batch too large for one launch");

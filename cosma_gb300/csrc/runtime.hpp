@@ -134,6 +134,10 @@ int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream,
                  cosma_gpu_ozaki_info* info);                    // ozaki2.cu
 int ozaki2_zgemm(const GemmDesc& g, int moduli, cudaStream_t stream,
                  cosma_gpu_ozaki_info* info);                    // ozaki2.cu
+// Free the per-stream workspaces of the precision forms before the stream is
+// destroyed (ozaki.cu, ozaki2.cu).
+void ozaki_release_stream(cudaStream_t s);
+void ozaki2_release_stream(cudaStream_t s);
 
 // The method of the process-wide entry points (p?gemm, multiply_using_layout):
 // cosma_gpu_pxgemm_set_method, else COSMA_GPU_GEMM_METHOD (pxgemm.cpp).

@@ -424,7 +424,11 @@ void cosma_gpu_tmm_destroy_context(cosma_gpu_mm_handle* h) {
         h->full_c.release();
         for (auto& kv : h->pinned) cudaHostUnregister((void*)kv.first);
         h->pinned.clear();
-        for (auto s : h->streams) cudaStreamDestroy(s);
+        for (auto s : h->streams) {
+            cgb::ozaki_release_stream(s);
+            cgb::ozaki2_release_stream(s);
+            cudaStreamDestroy(s);
+        }
         for (int i = 0; i < 2; ++i)
             for (cudaEvent_t e : {h->ev_ready[i], h->ev_free[i], h->ev_cin[i], h->ev_cdone[i], h->ev_cout[i]})
                 if (e) cudaEventDestroy(e);

@@ -235,6 +235,12 @@ int cosma_gpu_dgemm_ozaki2_residual(char transa, char transb, int64_t m, int64_t
  * device. */
 int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int exact_bits, int moduli, int* nmod,
                             int* fraction_bits);
+/* The precision forms keep a workspace per (device, stream) that grows to
+ * the largest problem run on that stream.  This frees the workspaces kept
+ * for `stream` on the current device; call it before destroying a stream
+ * that was passed to them (Tiled-MM handles do so for their own streams).
+ * Work on the stream must be complete.  Always succeeds. */
+int cosma_gpu_release_workspaces(void* stream);
 /* The same for complex double (interleaved re/im, op N, T or C): both parts
  * of C come out of one modular GEMM of depth 2k per modulus (four real
  * products per complex one), each part exact before its one rounding.

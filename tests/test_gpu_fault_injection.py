@@ -45,7 +45,8 @@ def test_workspace_allocation_failure_then_recovery(native_lib, cuda, site, meth
     want = to_dev(np.zeros((m, n)))
     fn("N", "N", m, n, k, 1.0, dA, m, dB, k, 0.0, want, m)
     torch.cuda.synchronize()
-    stream = torch.cuda.Stream()  # a new stream gets a new workspace: its first allocations run now
+    stream = torch.cuda.Stream()
+    cg.release_workspaces(stream)  # pooled streams are reused: start from no workspace, so allocations run now
     dC = to_dev(np.zeros((m, n)))
     native_lib.cosma_gpu_test_fail_next(site, 1)
     with pytest.raises(CosmaGpuError) as e:

@@ -28,7 +28,8 @@ def test_pack_bit_exact(native_lib, cuda, rows, cols, op, dtype):
     assert got.tobytes() == ref.tobytes()
 
 
-@pytest.mark.parametrize("alpha,beta", [(1.5, 0.5), (1.0, 0.0), (0.5, 1.0), (-2.0, -0.25)])
+@pytest.mark.parametrize("alpha,beta", [(1.5, 0.5), (1.0, 0.0), (0.5, 1.0), (-2.0, -0.25), (1.0, 0.3), (0.5, 0.0),
+                                        (-0.7, 1.0)])
 def test_unpack_real_bit_exact(native_lib, cuda, alpha, beta):
     from cosma_gb300 import unpack
     rows, cols = 129, 77
