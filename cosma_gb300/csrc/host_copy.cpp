@@ -280,7 +280,24 @@ int copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size
     return COSMA_GPU_SUCCESS;
 }
 
+int copy_2d_overlapped(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                       cudaMemcpyKind kind, cudaStream_t s) {
+    if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    const void* host = kind == cudaMemcpyHostToDevice ? src : dst;
+    const HostMem hm = host_mem(host);
+    if (hm == HostMem::PinnedMapped || hm == HostMem::PinnedOther) {
+        CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, s));
+        return COSMA_GPU_SUCCESS;
+    }
+    return copy_2d_async(dst, dpitch, src, spitch, width, cols, kind, s);
+}
+
 bool host_direct_available() { return host_direct(); }
+
+bool host_page_locked(const void* p) {
+    const HostMem hm = host_mem(p);
+    return hm == HostMem::PinnedMapped || hm == HostMem::PinnedOther;
+}
 
 }  // namespace cgb
 

@@ -56,6 +56,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace cgb {
 namespace oz2 {
@@ -998,6 +999,368 @@ int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
     return finish_info(info, w, pl, gp.kb_count);
 }
 
+// ------------------------------------------------------ host operands, overlapped
+// One-step DGEMM on host A, B and C (C = alpha op(A) op(B) + beta C), with the
+// host link's copies overlapped with the work: op(A) arrives in MA row panels
+// and op(B) in NB column panels on the copy stream, each panel's exponents
+// and statistics are taken as it lands, block (i, j)'s residue split and
+// modular GEMM start as soon as its two panels are in, and each block's C
+// leaves on its own stream while the next block computes.  The modulus count
+// is chosen from the first two panels and must be the one the whole data
+// gives (so the result is bit-identical to the device path's); it is checked
+// before any C is written, and when it differs, or the data holds Inf/NaN,
+// the call returns with *taken = false, C untouched and nothing in flight.
+struct PipeWorkspace {
+    DeviceBuffer a, b, resA, resB, expA, expB, part, R[2], C[2], stats, err;
+    Stats* host_stats = nullptr;  // one record per panel
+    unsigned* host_err = nullptr;
+    std::vector<cudaEvent_t> ev;
+    cudaStream_t ss = nullptr;  // exponents and statistics of landed panels, beside the GEMMs
+};
+
+std::mutex g_pipe_mu;
+std::map<std::pair<int, cudaStream_t>, PipeWorkspace*> g_pipe;
+constexpr int kPipeMaxPanels = 16;
+constexpr int kPipeEvents = 48;
+
+PipeWorkspace* pipe_workspace(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_pipe_mu);
+    auto& w = g_pipe[{dev, s}];
+    if (!w) w = new PipeWorkspace();
+    if (!w->host_stats && pinned_alloc((void**)&w->host_stats, kPipeMaxPanels * sizeof(Stats)) != cudaSuccess)
+        w->host_stats = nullptr;
+    if (!w->host_err && pinned_alloc((void**)&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
+    if (w->ev.empty()) {
+        w->ev.assign(kPipeEvents, nullptr);
+        for (auto& e : w->ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) e = nullptr;
+    }
+    if (!w->ss && cudaStreamCreateWithFlags(&w->ss, cudaStreamNonBlocking) != cudaSuccess) w->ss = nullptr;
+    cudaGetLastError();
+    return w;
+}
+
+void release_pipe_workspace(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    PipeWorkspace* w = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_pipe_mu);
+        auto it = g_pipe.find({dev, s});
+        if (it == g_pipe.end()) return;
+        w = it->second;
+        g_pipe.erase(it);
+    }
+    if (w->host_stats) cudaFreeHost(w->host_stats);
+    if (w->host_err) cudaFreeHost(w->host_err);
+    for (auto e : w->ev)
+        if (e) cudaEventDestroy(e);
+    if (w->ss) {
+        cudaStreamSynchronize(w->ss);
+        cudaStreamDestroy(w->ss);
+    }
+    delete w;
+    cudaGetLastError();
+}
+
+// Panel split of one dimension: `parts` pieces, each a multiple of 256 rows
+// (the CTA-pair tile) but the last.
+struct Panels {
+    int count = 1;
+    int64_t size = 0;
+    int64_t first(int i) const { return (int64_t)i * size; }
+    int64_t rows(int i, int64_t total) const { return std::min(size, total - first(i)); }
+};
+
+Panels make_panels(int64_t total, int parts) {
+    Panels p;
+    p.size = ceil_div(ceil_div(total, parts), 256) * 256;
+    p.count = (int)ceil_div(total, p.size);
+    return p;
+}
+
+// Combined statistics of a set of panel records (A panels in field 0, B in 1).
+Stats merge_stats(const Stats* s, const std::vector<int>& idx) {
+    Stats r{};
+    for (int i : idx) {
+        r.nonfinite |= s[i].nonfinite;
+        for (int w = 0; w < 2; ++w) {
+            r.spread[w] = std::max(r.spread[w], s[i].spread[w]);
+            r.exact_bits[w] = std::max(r.exact_bits[w], s[i].exact_bits[w]);
+        }
+    }
+    return r;
+}
+
+int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+                         cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
+    *taken = false;
+    const int64_t m = g.m, n = g.n, k = g.k;
+    if (g.scalar != Scalar::D || k > KMAX || k < 1 || m < 1 || n < 1) return COSMA_GPU_SUCCESS;
+    const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
+    const Panels PA = make_panels(m, m >= 2048 ? 2 : 1);
+    const Panels PB = make_panels(n, n >= 4096 ? 4 : (n >= 2048 ? 2 : 1));
+    const int MA = PA.count, NB = PB.count, NP = MA + NB;
+    if (MA * NB < 2 || NP > kPipeMaxPanels) return COSMA_GPU_SUCCESS;
+    PipeWorkspace* w = pipe_workspace(cs);
+    if (!w->host_stats || !w->host_err) return set_error(COSMA_GPU_ERROR_OUT_OF_MEMORY, "ozaki2: pinned staging");
+    for (auto e : w->ev)
+        if (!e) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: pipeline events");
+    if (!w->ss) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: pipeline stream");
+    cudaStream_t ss = w->ss;
+    const int64_t k_pad = ceil_div(k, BKE) * BKE;
+    const double* A = (const double*)g.A;
+    const double* B = (const double*)g.B;
+    double* C = (double*)g.C;
+    const bool beta_zero = g.beta[0] == 0.0;
+
+    // panel geometry: compact device copies, padded exponent / residue blocks
+    std::vector<int64_t> offA(MA), offB(NB), eoffA(MA), eoffB(NB);
+    int64_t a_elems = 0, b_elems = 0, ea = 0, eb = 0;
+    for (int i = 0; i < MA; ++i) {
+        offA[i] = a_elems; a_elems += PA.rows(i, m) * k;
+        eoffA[i] = ea; ea += ceil_div(PA.rows(i, m), 2 * BM) * 2 * BM;
+    }
+    for (int j = 0; j < NB; ++j) {
+        offB[j] = b_elems; b_elems += PB.rows(j, n) * k;
+        eoffB[j] = eb; eb += ceil_div(PB.rows(j, n), BN) * BN;
+    }
+    const int64_t ma_pad = ceil_div(PA.size, 2 * BM) * 2 * BM, nb_pad = ceil_div(PB.size, BN) * BN;
+    // everything that could allocate is reserved before the first copy: a
+    // growing buffer frees its old memory, which waits for the whole device
+    CGB_CHECK(w->a.reserve((size_t)a_elems * 8, cs));
+    CGB_CHECK(w->b.reserve((size_t)b_elems * 8, cs));
+    CGB_CHECK(w->expA.reserve((size_t)ea * 4, cs));
+    CGB_CHECK(w->expB.reserve((size_t)eb * 4, cs));
+    CGB_CHECK(w->part.reserve((size_t)64 * std::max(PA.size, PB.size) * 12, cs));
+    for (auto& c : w->C) CGB_CHECK(c.reserve((size_t)PA.size * PB.size * 8, cs));
+    CGB_CHECK(w->stats.reserve((size_t)NP * sizeof(Stats), cs));
+    CGB_CHECK(w->err.reserve(sizeof(unsigned), cs));
+    Stats* sdev = (Stats*)w->stats.ptr;
+    double* dA = (double*)w->a.ptr;
+    double* dB = (double*)w->b.ptr;
+    int* expA = (int*)w->expA.ptr;
+    int* expB = (int*)w->expB.ptr;
+    CGB_CUDA(cudaMemsetAsync(sdev, 0, (size_t)NP * sizeof(Stats), cs));
+    CGB_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(unsigned), cs));
+    CGB_CUDA(cudaMemsetAsync(expA, 0, (size_t)ea * 4, cs));
+    CGB_CUDA(cudaMemsetAsync(expB, 0, (size_t)eb * 4, cs));
+    CGB_CUDA(cudaStreamSynchronize(cs));
+    int evi = 0;
+    auto next_event = [&]() { return w->ev[evi++]; };
+    cudaEvent_t ev_copy[kPipeMaxPanels];    // panel p landed in HBM (A panels 0..MA-1, B panels MA..)
+    cudaEvent_t ev_scaled[kPipeMaxPanels];  // its exponents and statistics are in
+    *h2d_bytes = 0;
+    *d2h_bytes = 0;
+
+    // device copy of op(A) rows / op(B) columns of one panel, compact
+    auto copy_panel = [&](int p) -> int {
+        if (p < MA) {
+            const int64_t i0 = PA.first(p), mi = PA.rows(p, m);
+            if (!a_kc) CGB_CHECK(copy_2d_overlapped(dA + offA[p], mi * 8, A + i0, g.lda * 8, mi * 8, k,
+                                                    cudaMemcpyHostToDevice, hs));
+            else CGB_CHECK(copy_2d_overlapped(dA + offA[p], k * 8, A + i0 * g.lda, g.lda * 8, k * 8, mi,
+                                              cudaMemcpyHostToDevice, hs));
+            *h2d_bytes += mi * k * 8;
+        } else {
+            const int j = p - MA;
+            const int64_t j0 = PB.first(j), nj = PB.rows(j, n);
+            if (b_kc) CGB_CHECK(copy_2d_overlapped(dB + offB[j], k * 8, B + j0 * g.ldb, g.ldb * 8, k * 8, nj,
+                                                   cudaMemcpyHostToDevice, hs));
+            else CGB_CHECK(copy_2d_overlapped(dB + offB[j], nj * 8, B + j0, g.ldb * 8, nj * 8, k,
+                                              cudaMemcpyHostToDevice, hs));
+            *h2d_bytes += nj * k * 8;
+        }
+        ev_copy[p] = next_event();
+        CGB_CUDA(cudaEventRecord(ev_copy[p], hs));
+        return COSMA_GPU_SUCCESS;
+    };
+    // exponents and statistics of one panel as soon as it lands, on the
+    // statistics stream (small kernels that run beside the GEMMs)
+    auto scale_panel = [&](int p) -> int {
+        CGB_CUDA(cudaStreamWaitEvent(ss, ev_copy[p], 0));
+        if (p < MA) {
+            const int64_t mi = PA.rows(p, m);
+            CGB_CHECK(oz::scale_operand(a_kc, dA + offA[p], a_kc ? k : mi, mi, k, expA + eoffA[p], w->part, sdev + p,
+                                        0, ss, 1));
+        } else {
+            const int j = p - MA;
+            const int64_t nj = PB.rows(j, n);
+            CGB_CHECK(oz::scale_operand(b_kc, dB + offB[j], b_kc ? k : nj, nj, k, expB + eoffB[j], w->part,
+                                        sdev + p, 1, ss, 1));
+        }
+        ev_scaled[p] = next_event();
+        CGB_CUDA(cudaEventRecord(ev_scaled[p], ss));
+        return COSMA_GPU_SUCCESS;
+    };
+    // drains every stream (the caller then runs the regular path)
+    auto abandon = [&]() -> int {
+        for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));
+        *h2d_bytes = 0;
+        return COSMA_GPU_SUCCESS;
+    };
+
+    // 1. the first panels of each operand; the modulus count from them
+    CGB_CUDA(cudaStreamSynchronize(ss));  // memsets on cs above: ss starts after them
+    CGB_CHECK(copy_panel(0));
+    CGB_CHECK(copy_panel(MA));
+    CGB_CHECK(scale_panel(0));
+    CGB_CHECK(scale_panel(MA));
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, sdev, (size_t)NP * sizeof(Stats), cudaMemcpyDeviceToHost, ss));
+    CGB_CUDA(cudaStreamSynchronize(ss));
+    const Stats s0 = merge_stats(w->host_stats, {0, MA});
+    if (s0.nonfinite) return abandon();
+    Plan pl;
+    pl.spread = (double)s0.spread[0] + (double)s0.spread[1];
+    if (choose(nmod_req, pl.spread, k, &pl.nmod, &pl.P, std::max(s0.exact_bits[0], s0.exact_bits[1])) !=
+        COSMA_GPU_SUCCESS) {
+        clear_error();
+        return abandon();
+    }
+    const int N = pl.nmod;
+    std::vector<int64_t> roffA(MA), roffB(NB);
+    int64_t ra = 0, rb = 0;
+    for (int i = 0; i < MA; ++i) { roffA[i] = ra; ra += (int64_t)N * ceil_div(PA.rows(i, m), 2 * BM) * 2 * BM * k_pad; }
+    for (int j = 0; j < NB; ++j) { roffB[j] = rb; rb += (int64_t)N * ceil_div(PB.rows(j, n), BN) * BN * k_pad; }
+    CGB_CHECK(w->resA.reserve((size_t)ra * 2, cs));  // nothing in flight: the first panels are in
+    CGB_CHECK(w->resB.reserve((size_t)rb * 2, cs));
+    for (auto& r : w->R) CGB_CHECK(r.reserve((size_t)N * ma_pad * nb_pad, cs));
+
+    // 2. the other panels: B's first (block row 0 uses them), then A's; each
+    // is scaled as it lands
+    for (int p = MA + 1; p < NP; ++p) CGB_CHECK(copy_panel(p));
+    for (int p = 1; p < MA; ++p) CGB_CHECK(copy_panel(p));
+    for (int p = MA + 1; p < NP; ++p) CGB_CHECK(scale_panel(p));
+    for (int p = 1; p < MA; ++p) CGB_CHECK(scale_panel(p));
+    cudaEvent_t ev_stats = next_event();
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, sdev, (size_t)NP * sizeof(Stats), cudaMemcpyDeviceToHost, ss));
+    CGB_CUDA(cudaEventRecord(ev_stats, ss));
+
+    SplitParams sp;
+    fill_split(sp, N, pl.P);
+    std::vector<char> split_done(NP, 0);
+    auto split_panel = [&](int p) -> int {
+        if (split_done[p]) return COSMA_GPU_SUCCESS;
+        split_done[p] = 1;
+        CGB_CUDA(cudaStreamWaitEvent(cs, ev_scaled[p], 0));
+        if (p < MA) {
+            const int64_t mi = PA.rows(p, m), mi_pad = ceil_div(mi, 2 * BM) * 2 * BM;
+            const dim3 grid((unsigned)(mi_pad / 32), (unsigned)(k_pad / 64));
+            launch_split(a_kc, dA + offA[p], a_kc ? k : mi, mi, k, expA + eoffA[p], k_pad, mi_pad,
+                         (uint16_t*)w->resA.ptr + roffA[p], sp, grid, cs);
+        } else {
+            const int j = p - MA;
+            const int64_t nj = PB.rows(j, n), nj_pad = ceil_div(nj, BN) * BN;
+            const dim3 grid((unsigned)(nj_pad / 32), (unsigned)(k_pad / 64));
+            launch_split(b_kc, dB + offB[j], b_kc ? k : nj, nj, k, expB + eoffB[j], k_pad, nj_pad,
+                         (uint16_t*)w->resB.ptr + roffB[j], sp, grid, cs);
+        }
+        CGB_CUDA(cudaGetLastError());
+        return COSMA_GPU_SUCCESS;
+    };
+    // block b = i NB + j (row-major): its residue bytes go to R[b % 2], which
+    // the reconstruction of block b - 2 has read by then (same stream)
+    auto gemm_block = [&](int b) -> int {
+        const int i = b / NB, j = b % NB;
+        CGB_CHECK(split_panel(i));
+        CGB_CHECK(split_panel(MA + j));
+        const int64_t mi_pad = ceil_div(PA.rows(i, m), 2 * BM) * 2 * BM;
+        const int64_t nj_pad = ceil_div(PB.rows(j, n), BN) * BN;
+        GemmParams gp;
+        fill_gemm(gp, N, mi_pad, nj_pad, k_pad, w->R[b & 1].ptr, (unsigned*)w->err.ptr);
+        return launch_gemm((uint16_t*)w->resA.ptr + roffA[i], (uint16_t*)w->resB.ptr + roffB[j], k_pad, gp, cs);
+    };
+
+    // 3. the first two blocks start while the other panels are on the way
+    // (two, so that a slow link leaves the GPU work until the last panel is in)
+    const int NBLK = MA * NB;
+    CGB_CHECK(gemm_block(0));
+    CGB_CHECK(gemm_block(1));
+    // every panel's statistics, then the check that the first panels chose
+    // the modulus count the whole data gives
+    CGB_CUDA(cudaEventSynchronize(ev_stats));
+    std::vector<int> all(NP);
+    for (int p = 0; p < NP; ++p) all[p] = p;
+    const Stats sa = merge_stats(w->host_stats, all);
+    if (sa.nonfinite) return abandon();
+    Plan full;
+    full.spread = (double)sa.spread[0] + (double)sa.spread[1];
+    const int exact_bits = std::max(sa.exact_bits[0], sa.exact_bits[1]);
+    if (choose(nmod_req, full.spread, k, &full.nmod, &full.P, exact_bits) != COSMA_GPU_SUCCESS) {
+        clear_error();
+        return abandon();
+    }
+    if (full.nmod != N || full.P != pl.P) return abandon();
+    full.exact = full.P >= exact_bits;
+
+    // 4. blocks in order; block b's C leaves on ds while block b+1 computes
+    CombineParams cp0;
+    fill_combine(cp0, N, pl.P);
+    cudaEvent_t ev_comb[2] = {next_event(), next_event()}, ev_out[2] = {next_event(), next_event()},
+                ev_cin[2] = {next_event(), next_event()};
+    bool out_used[2] = {false, false};
+    for (int b = 0; b < NBLK; ++b) {
+        {
+            const int i = b / NB, j = b % NB;
+            const int64_t i0 = PA.first(i), mi = PA.rows(i, m), j0 = PB.first(j), nj = PB.rows(j, n);
+            const int slot = b & 1;
+            double* cdev = (double*)w->C[slot].ptr;
+            if (!beta_zero) {  // the old C block comes in once its slot has been drained
+                if (out_used[slot]) CGB_CUDA(cudaStreamWaitEvent(hs, ev_out[slot], 0));
+                CGB_CHECK(copy_2d_overlapped(cdev, mi * 8, C + i0 + j0 * g.ldc, g.ldc * 8, mi * 8, nj,
+                                             cudaMemcpyHostToDevice, hs));
+                *h2d_bytes += mi * nj * 8;
+                CGB_CUDA(cudaEventRecord(ev_cin[slot], hs));
+                CGB_CUDA(cudaStreamWaitEvent(cs, ev_cin[slot], 0));
+            } else if (out_used[slot]) {
+                CGB_CUDA(cudaStreamWaitEvent(cs, ev_out[slot], 0));
+            }
+            CombineParams cp = cp0;
+            cp.m = mi;
+            cp.n = nj;
+            cp.ldc = mi;
+            cp.m_pad = ceil_div(mi, 2 * BM) * 2 * BM;
+            cp.nb16 = ceil_div(nj, BN) * BN / 16;
+            cp.n_split = INT64_MAX;
+            cp.cs = 1;
+            cp.R = (const uint8_t*)w->R[b & 1].ptr;
+            cp.expA = expA + eoffA[i];
+            cp.expB = expB + eoffB[j];
+            cp.C = cdev;
+            cp.alpha = g.alpha[0];
+            cp.beta = g.beta[0];
+            cp.alpha_one = g.alpha[0] == 1.0;
+            cp.beta_zero = beta_zero;
+            CGB_CHECK(launch_combine(cp, N, nj, cs));
+            CGB_CUDA(cudaEventRecord(ev_comb[slot], cs));
+            CGB_CUDA(cudaStreamWaitEvent(ds, ev_comb[slot], 0));
+            CGB_CHECK(copy_2d_overlapped(C + i0 + j0 * g.ldc, g.ldc * 8, cdev, mi * 8, mi * 8, nj,
+                                         cudaMemcpyDeviceToHost, ds));
+            *d2h_bytes += mi * nj * 8;
+            CGB_CUDA(cudaEventRecord(ev_out[slot], ds));
+            out_used[slot] = true;
+        }
+        if (b + 2 < NBLK) CGB_CHECK(gemm_block(b + 2));  // after this block's reconstruction freed its R
+    }
+    *taken = true;
+    for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));
+    CGB_CUDA(cudaMemcpy(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (*w->host_err)
+        return set_error(COSMA_GPU_ERROR_DEVICE_TIMEOUT,
+                         "ozaki2 gemm: a pipeline wait timed out (device code " + std::to_string(*w->host_err) + ")");
+    if (info) {
+        info->slices = N;
+        info->products = N;
+        info->fraction_bits = pl.P;
+        info->exact_product = full.exact ? 1 : 0;
+        info->groups = N * (int)ceil_div(k_pad / BKE, KB_PER_CHUNK);
+        info->spread_bits = full.spread;
+    }
+    return COSMA_GPU_SUCCESS;
+}
+
 }  // namespace oz2
 
 }  // namespace cgb
@@ -1040,7 +1403,18 @@ extern "C" int cosma_gpu_ozaki2_choose(int64_t k, double spread_bits, int exact_
 
 namespace cgb {
 
-void ozaki2_release_stream(cudaStream_t s) { oz2::release_workspace(s); }
+void ozaki2_release_stream(cudaStream_t s) {
+    oz2::release_workspace(s);
+    oz2::release_pipe_workspace(s);
+}
+
+int ozaki2_dgemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+                      cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
+    *taken = false;
+    if (((uintptr_t)g.A | (uintptr_t)g.B | (uintptr_t)g.C) % 8) return COSMA_GPU_SUCCESS;
+    if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24) return COSMA_GPU_SUCCESS;
+    return oz2::dgemm_host_pipelined(g, moduli, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
+}
 
 int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_ozaki_info* info) {
     if (g.scalar != Scalar::D) return set_error(COSMA_GPU_ERROR_NOT_SUPPORTED, "ozaki2: double only");

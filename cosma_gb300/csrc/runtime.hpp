@@ -138,6 +138,14 @@ int ozaki2_zgemm(const GemmDesc& g, int moduli, cudaStream_t stream,
 // destroyed (ozaki.cu, ozaki2.cu).
 void ozaki_release_stream(cudaStream_t s);
 void ozaki2_release_stream(cudaStream_t s);
+// One-step DGEMM on host A, B, C with the host copies overlapped with the
+// Chinese-remainder work (ozaki2.cu): cs computes, hs carries host-to-device
+// copies, ds device-to-host copies.  *taken = false (C untouched, nothing in
+// flight) when the shape does not pipeline, or when the first panels'
+// modulus count differs from the whole data's or the data holds Inf/NaN:
+// the caller then runs the regular path.
+int ozaki2_dgemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+                      cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken);
 
 // The method of the process-wide entry points (p?gemm, multiply_using_layout):
 // cosma_gpu_pxgemm_set_method, else COSMA_GPU_GEMM_METHOD (pxgemm.cpp).
@@ -158,6 +166,13 @@ int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
 // own staging).  Nothing is waited for.
 int copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                   cudaMemcpyKind kind, cudaStream_t s);
+// The same, for copies that overlap a running persistent kernel: page-locked
+// host memory goes through the copy engines (at the link's rate, without
+// taking SMs from the kernel: copy kernels beside the modular GEMM, whether
+// a full grid or 64 CTAs, held a 16384^3 call at ~120 ms against ~100 ms),
+// pageable memory as in copy_2d_async.
+int copy_2d_overlapped(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                       cudaMemcpyKind kind, cudaStream_t s);
 // Whether the device copy kernel route is on (capable device, and
 // COSMA_GPU_HOST_DIRECT not OFF).
 bool host_direct_available();
@@ -165,6 +180,8 @@ bool host_direct_available();
 // place (pageable or mapped pinned memory on a host whose page tables the
 // device uses); pageable pages are faulted in on the host first.
 bool prepare_direct_host(void* p, size_t pitch, size_t width, size_t cols, bool write);
+// Whether p is page-locked host memory (host_copy.cpp).
+bool host_page_locked(const void* p);
 
 // Grouped Ozaki-split FP64 GEMM (ozaki_grouped.cu), driven by the grouped
 // plan of grouped.cu when it is created with the Ozaki method.

@@ -227,11 +227,37 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     const int64_t ntm = ceil_div(m, tm), ntn = ceil_div(n, tn), ntk = trivial ? 1 : ceil_div(k, tk);
     const int64_t ntiles = ntm * ntn, nsteps = ntiles * ntk;
     const bool keep_on_device = !dC && !copy_c_back;
+    const bool crt = h->method == COSMA_GPU_METHOD_OZAKI2 && (sc == Scalar::D || sc == Scalar::Z);
+    // One step on page-locked host operands with the Chinese-remainder
+    // method: the overlapped form (op(A) / op(B) panels copied by the copy
+    // engines while earlier blocks compute, C blocks copied out while later
+    // ones do) where it applies; 16384^3 took 99.5 to 101 ms per call in it
+    // against 116 ms in the one-step form.  Pageable arrays keep the one-step
+    // form: copy kernels beside the modular GEMM cost it as much as they save.
+    const bool overlap = env_bool("COSMA_GPU_OZAKI2_OVERLAP", true);
+    // With two streams the C blocks leave on the copy stream, behind every
+    // panel copy (those end long before the first block is reconstructed).
+    if (overlap && crt && sc == Scalar::D && !dA && !dB && !dC && !trivial && !keep_on_device && nsteps == 1 &&
+        h->streams.size() >= 2 && host_page_locked(A) && host_page_locked(B) && host_page_locked(C)) {
+        const GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        cosma_gpu_ozaki_info oi{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
+        int64_t h2d = 0, d2h = 0;
+        bool taken = false;
+        const size_t S = h->streams.size();
+        CGB_CHECK(ozaki2_dgemm_host(g, h->slices, h->streams[0], h->streams[1], h->streams[std::min<size_t>(2, S - 1)],
+                                    &oi, &h2d, &d2h, &taken));
+        if (taken) {
+            *info = oi;
+            h->last_h2d_bytes = h2d;
+            h->last_d2h_bytes = d2h;
+            h->last_device_c = nullptr;
+            return COSMA_GPU_SUCCESS;
+        }
+    }
     // One step with the Chinese-remainder method: its reconstruction kernel
     // writes (and, for beta != 0, reads) C in host memory directly where the
     // device reaches it, so the write-back overlaps that kernel instead of
     // following it as a separate copy, and no C slot is needed.
-    const bool crt = h->method == COSMA_GPU_METHOD_OZAKI2 && (sc == Scalar::D || sc == Scalar::Z);
     const bool direct_c = crt && !dC && !keep_on_device && !trivial && nsteps == 1 &&
                           prepare_direct_host(C, (size_t)ldc * es, (size_t)m * es, (size_t)n, true);
     for (int s = 0; s < R; ++s) {
@@ -331,7 +357,7 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
                                         cdev, cld);
             cosma_gpu_ozaki_info ti_info;
             CGB_CHECK(gemm_device(g, h->method, h->slices, cs, &ti_info));
-            if (ti_info.slices) *info = ti_info;
+            if (ti_info.slices || ti_info.fallback_native) *info = ti_info;
             CGB_CUDA(cudaEventRecord(ev_free[r], cs));
         }
         if (kt == ntk - 1 && direct_c) h->last_d2h_bytes += mi * nj * es;  // written in place by the GEMM

@@ -253,3 +253,85 @@ def test_tiled_mm_one_step_c_in_place(native_lib, cuda, monkeypatch, scalar):
     for got in outs:
         np.testing.assert_array_equal(got[:m], want)
         np.testing.assert_array_equal(got[m:], C0[m:])  # rows past m untouched
+
+
+def _host_matrix(A, pinned):
+    """Column-major host copy of A, pageable numpy or page-locked torch memory."""
+    import torch
+    if not pinned:
+        return np.asfortranarray(A), None
+    t = torch.from_numpy(np.ascontiguousarray(A.T).reshape(-1)).pin_memory()  # column-major flat
+    return t, t
+
+
+def _tmm_call(ta, tb, m, n, k, A, B, C0, alpha, beta, ldc, pinned, overlap, monkeypatch, moduli=0, streams=3):
+    from cosma_gb300 import gemm, make_context
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "ON" if overlap else "OFF")
+    hA, _ = _host_matrix(A, pinned)
+    hB, _ = _host_matrix(B, pinned)
+    Cfull = np.zeros((ldc, n))
+    Cfull[:m] = C0
+    hC, tC = _host_matrix(Cfull, pinned)
+    h = make_context("d", streams)
+    h.set_method("ozaki2", moduli)
+    gemm(h, ta, tb, m, n, k, alpha, hA, A.shape[0], hB, B.shape[0], beta, hC, ldc)
+    moved = h.transfer_bytes()
+    info = h.ozaki_info()
+    h.close()
+    out = tC.numpy().reshape(n, ldc).T if tC is not None else hC
+    return np.array(out), moved, info
+
+
+@pytest.mark.parametrize("ta,tb,beta", [("N", "N", 0.0), ("T", "N", 0.5), ("N", "T", -1.0), ("T", "T", 0.0)])
+def test_tiled_mm_overlapped_panels(native_lib, cuda, monkeypatch, ta, tb, beta):
+    """One-step Tiled-MM calls on page-locked arrays large enough for the
+    overlapped form (2 x 2 panels: op(A) rows and op(B) columns arrive while
+    earlier blocks compute): the bits of the one-step form without overlap and
+    of the device-pointer call; transfers count A and B (and C, when it is
+    read) once.  Handles with two streams carry the C blocks on the copy
+    stream.  The overlapped form times no phases (gemm_ms stays 0), which
+    tells it from the one-step form; pageable arrays keep the one-step form."""
+    pinned = True
+    m, n, k = 2100, 2300, 300
+    ldc = m + 3
+    A = oracle.exp_spread(_op_shape(ta, m, k), 71, 4)
+    B = oracle.exp_spread(_op_shape(tb, k, n), 72, 4)
+    C0 = oracle.uniform((m, n), 73)
+    alpha = 0.75
+    on, moved, info = _tmm_call(ta, tb, m, n, k, A, B, C0, alpha, beta, ldc, pinned, True, monkeypatch,
+                                streams=2 if beta != 0 else 3)
+    off, _, info_off = _tmm_call(ta, tb, m, n, k, A, B, C0, alpha, beta, ldc, pinned, False, monkeypatch)
+    np.testing.assert_array_equal(on[:m], off[:m])
+    np.testing.assert_array_equal(on[m:], np.zeros((ldc - m, n)))  # rows past m untouched
+    assert info["slices"] == info_off["slices"] and info["fraction_bits"] == info_off["fraction_bits"]
+    assert info["gemm_ms"] == 0.0 and info_off["gemm_ms"] > 0.0
+    _, _, info_pg = _tmm_call(ta, tb, m, n, k, A, B, C0, alpha, beta, ldc, False, True, monkeypatch)
+    assert info_pg["gemm_ms"] > 0.0
+    assert moved == (8 * (m * k + k * n + (m * n if beta != 0 else 0)), 8 * m * n)
+    from cosma_gb300 import dgemm_ozaki2_device
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C0, ldc)
+    dgemm_ozaki2_device(ta, tb, m, n, k, alpha, dA, A.shape[0], dB, B.shape[0], beta, dC, ldc)
+    np.testing.assert_array_equal(on[:m], from_dev(dC, m, n, ldc))
+
+
+@pytest.mark.parametrize("case", ["wide_spread_late", "nan_late"])
+def test_tiled_mm_overlapped_falls_back(native_lib, cuda, monkeypatch, case):
+    """The modulus count is chosen from the first panels: when a later panel
+    needs more (a wider exponent spread in op(B)'s last columns) or holds NaN,
+    the overlapped form gives way before writing C and the regular one-step
+    path runs: the same bits as with the overlap switched off."""
+    m, n, k = 2100, 2300, 300
+    A = oracle.exp_spread((m, k), 81, 0)
+    B = oracle.exp_spread((k, n), 82, 0)
+    if case == "wide_spread_late":
+        B[:, -500:] = oracle.exp_spread((k, 500), 83, 40)
+    else:
+        A[-3, 7] = np.nan
+    C0 = np.zeros((m, n))
+    on, _, info = _tmm_call("N", "N", m, n, k, A, B, C0, 1.0, 0.0, m, True, True, monkeypatch)
+    off, _, info_off = _tmm_call("N", "N", m, n, k, A, B, C0, 1.0, 0.0, m, True, False, monkeypatch)
+    np.testing.assert_array_equal(np.isnan(on), np.isnan(off))
+    np.testing.assert_array_equal(np.nan_to_num(on), np.nan_to_num(off))
+    for key in ("slices", "fraction_bits", "exact_product", "fallback_native"):
+        assert info[key] == info_off[key]
+    assert info["fallback_native"] == (1 if case == "nan_late" else 0)
