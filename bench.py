@@ -838,7 +838,9 @@ def cfg_stream(steps, warmup, n=16384, tile=8192):
                                    f"(Chinese-remainder form), streamed from pinned host memory",
                        "scaled_down_from": "65536^3 (206 GB of host matrices, beyond the host's memory)"},
             "moduli": nmod, "h2d_bytes": h2d, "d2h_bytes": d2h,
-            "link": {"h2d_GBs_measured": h2d_gbs, "d2h_GBs_measured": d2h_gbs, "host_copy_route": route,
+            "link": {"h2d_GBs_measured": h2d_gbs, "d2h_GBs_measured": d2h_gbs,
+                     "tile_copies": "copy engines (page-locked host buffers; the in-place copy kernel, route "
+                                    f"{route} for standalone copies, would hold SMs the tile GEMMs wait for)",
                      "link_GBs_achieved": (h2d + d2h) / wall / 1e9},
             "compute_alone_s": compute_s, "link_alone_s": link_s, "overlap_efficiency": max(compute_s, link_s) / wall,
             "accuracy": {"max_rel_err": float(max(rel)), "samples": len(rel),
@@ -846,8 +848,8 @@ def cfg_stream(steps, warmup, n=16384, tile=8192):
             "roofline": {"bound": "tensor" if tensor_s >= link_s else "host-link",
                          "achieved": flops / wall / 1e12, "unit": "TFLOP/s",
                          "peak": flops / bound_s / 1e12, "frac": bound_s / wall, "traffic": h2d + d2h,
-                         "kernel": f"streamer: host copies by route '{route}' on two streams overlapped with the "
-                                   "Chinese-remainder GEMM",
+                         "kernel": "streamer: tile copies by the copy engines on two streams overlapped with "
+                                   "the Chinese-remainder GEMM",
                          "peak_note": f"the slower of tensor time ({nmod} BF16 GEMMs of 8mnk flops at the {pk_kind} "
                                       f"sustained BF16 rate) and link time (bytes at the link rates measured in "
                                       f"this run)"},

@@ -116,10 +116,13 @@ size_t span_bytes(int64_t rows, int64_t cols, int64_t ld, size_t es) {
     return ((size_t)(cols - 1) * (size_t)ld + (size_t)rows) * es;
 }
 
+// Tile copies run beside the GEMMs of other steps: page-locked host memory
+// goes through the copy engines (copy kernels would hold SMs the persistent
+// GEMMs wait for), pageable memory through the in-place copy kernel.
 int copy2d(void* dst, int64_t dld, const void* src, int64_t sld, int64_t rows, int64_t cols, size_t es,
            cudaMemcpyKind kind, cudaStream_t s) {
     if (rows == 0 || cols == 0) return COSMA_GPU_SUCCESS;
-    return copy_2d_async(dst, (size_t)dld * es, src, (size_t)sld * es, (size_t)rows * es, (size_t)cols, kind, s);
+    return copy_2d_overlapped(dst, (size_t)dld * es, src, (size_t)sld * es, (size_t)rows * es, (size_t)cols, kind, s);
 }
 
 bool is_zero(const double* v, Scalar s) { return v[0] == 0.0 && (!scalar_complex(s) || v[1] == 0.0); }
