@@ -143,24 +143,76 @@ __device__ __forceinline__ float mul_pow2(float s, int e, float x) {
     return __int_as_float(b + (e << 23));
 }
 
+// fl(s * x) for a double s = +-m 2^e with an odd significand m of at most 11
+// bits (1.5, 3, 0.75, ...): the 53-bit significand of x times m fits 64 bits,
+// and its round-to-nearest-even to 53 bits with the exponents added is the
+// IEEE product whenever that product is a normal number.  A zero x gives the
+// signed zero; subnormal x, Inf/NaN and products outside the normal range
+// take the multiply (rare: a call).  Integer work only, so that the unpack
+// issues one FP64 instruction per element (the add) instead of two.
+// With k = floor(log2 m), the product P = (2^52 + frac) m has its top bit at
+// 52 + k or 53 + k, so one shift finds how many bits (sh) fall below the kept
+// 53, and P + 2^(sh-1) - 1 + (bit sh of P), shifted by sh, is P rounded to
+// nearest even.
+__device__ __forceinline__ double mul_short(double s, uint32_t m, int e, int k, double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long sign = (b ^ (unsigned long long)__double_as_longlong(s)) & 0x8000000000000000ull;
+    const int ex = (int)((b >> 52) & 0x7FF);
+    if ((unsigned)(ex - 1) >= 0x7FEu) {  // zero, subnormal, Inf or NaN
+        if ((b << 1) == 0) return __longlong_as_double((long long)sign);
+        return mul_rare(s, x);
+    }
+    const unsigned long long P = ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) * m;  // < 2^(54 + k)
+    const int sh = k + (int)(P >> (53 + k));                                      // 0..11
+    const unsigned long long lsb = (P >> sh) & 1ull;
+    const unsigned long long bias = sh ? (1ull << (sh - 1)) - 1ull + lsb : 0ull;
+    unsigned long long q = (P + bias) >> sh;
+    int ne = ex + e + sh;
+    const int carry = (int)(q >> 53);  // rounding carried into a new bit
+    q >>= carry;
+    ne += carry;
+    if ((unsigned)(ne - 1) >= 0x7FEu) return mul_rare(s, x);  // product outside the normal range
+    return __longlong_as_double((long long)(sign | ((unsigned long long)ne << 52) | (q & 0xFFFFFFFFFFFFFull)));
+}
+
 // How a real scale is applied: 0 = identity (s == 1), 1 = exponent shift
-// (s a power of two, exponent e), 2 = multiply.
+// (s a power of two, exponent e), 2 = multiply, 3 = short-significand
+// product (double only: s = +-m 2^e, m odd, at most 11 bits).
 template <class R>
 struct ScaleMode {
     int mode, e;
+    uint32_t m;
+    int k;  // floor(log2 m)
 };
 template <class R>
 __host__ ScaleMode<R> scale_mode(double s) {
     int e = 0;
     const double f = std::frexp(s, &e);  // s = f * 2^e, f in [0.5, 1)
-    if (s == 1.0) return {0, 0};
-    if (f == 0.5 && std::isfinite(s)) return {1, e - 1};
-    return {2, 0};
+    if (s == 1.0) return {0, 0, 1, 0};
+    if (f == 0.5 && std::isfinite(s)) return {1, e - 1, 1, 0};
+    if (sizeof(R) == 8 && std::isfinite(s) && s != 0.0) {
+        double a = std::fabs(f);
+        int ae = e;
+        for (int i = 0; i < 11 && a != std::floor(a); ++i) {  // a * 2^ae == |s|; make a an integer
+            a *= 2.0;
+            --ae;
+        }
+        if (a == std::floor(a) && a < 2048.0) {
+            int k = 0;
+            while ((2u << k) <= (uint32_t)a) ++k;
+            return {3, ae, (uint32_t)a, k};
+        }
+    }
+    return {2, 0, 1, 0};
 }
 template <int MODE, class R>
-__device__ __forceinline__ R apply_scale(R s, int e, R x) {
+__device__ __forceinline__ R apply_scale(R s, const ScaleMode<R>& md, R x) {
     if constexpr (MODE == 0) return x;
-    else if constexpr (MODE == 1) return mul_pow2(s, e, x);
+    else if constexpr (MODE == 1) return mul_pow2(s, md.e, x);
+    else if constexpr (MODE == 3) {
+        if constexpr (sizeof(R) == 8) return mul_short(s, md.m, md.e, md.k, x);
+        else return mul_rn(s, x);  // not chosen for float
+    }
     else return mul_rn(s, x);
 }
 
@@ -177,8 +229,8 @@ __device__ __forceinline__ R apply_scale(R s, int e, R x) {
 // with runtime modes the compiler issues every mode's FP64 multiply,
 // predicated, for every element.
 template <class R, int AM, int BM, bool READ>
-__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, int ae, const R* __restrict__ src,
-                                   int64_t lds, R beta, int be, R* __restrict__ dst, int64_t ldd) {
+__global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, ScaleMode<R> am, const R* __restrict__ src,
+                                   int64_t lds, R beta, ScaleMode<R> bm, R* __restrict__ dst, int64_t ldd) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t j = blockIdx.y; j < cols; j += gridDim.y) {
         const R* s = src + j * lds;
@@ -195,8 +247,45 @@ __global__ void unpack_real_kernel(int64_t rows, int64_t cols, R alpha, int ae, 
             for (int q = 0; q < 4; ++q) {
                 const int64_t i = i0 + q * stride;
                 if (i >= rows) break;
-                R v = apply_scale<AM>(alpha, ae, x[q]);
-                if constexpr (READ) v = add_rn(v, apply_scale<BM>(beta, be, y[q]));
+                R v = apply_scale<AM>(alpha, am, x[q]);
+                if constexpr (READ) v = add_rn(v, apply_scale<BM>(beta, bm, y[q]));
+                d[i] = v;
+            }
+        }
+    }
+}
+
+// The same on 16-byte pairs of doubles (rows, leading dimensions even and
+// both arrays 16-byte aligned): a warp moves 512 bytes per load instead of
+// 256, which the unpack needs to keep HBM busy once its FP64 work is one
+// instruction per element.
+template <int AM, int BM, bool READ>
+__global__ void unpack_real2_kernel(int64_t rows2, int64_t cols, double alpha, ScaleMode<double> am,
+                                    const double2* __restrict__ src, int64_t lds2, double beta, ScaleMode<double> bm,
+                                    double2* __restrict__ dst, int64_t ldd2) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = blockIdx.y; j < cols; j += gridDim.y) {
+        const double2* s = src + j * lds2;
+        double2* d = dst + j * ldd2;
+        for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < rows2; i0 += 4 * stride) {
+            double2 x[4], y[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t i = i0 + q * stride;
+                x[q] = i < rows2 ? s[i] : make_double2(0.0, 0.0);
+                y[q] = (READ && i < rows2) ? d[i] : make_double2(0.0, 0.0);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int64_t i = i0 + q * stride;
+                if (i >= rows2) break;
+                double2 v;
+                v.x = apply_scale<AM>(alpha, am, x[q].x);
+                v.y = apply_scale<AM>(alpha, am, x[q].y);
+                if constexpr (READ) {
+                    v.x = add_rn(v.x, apply_scale<BM>(beta, bm, y[q].x));
+                    v.y = add_rn(v.y, apply_scale<BM>(beta, bm, y[q].y));
+                }
                 d[i] = v;
             }
         }
@@ -301,20 +390,39 @@ int pack_device(int op, bool is_complex, int elem_bytes, int64_t rows, int64_t c
     return set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "pack: elem_bytes must be 4, 8 or 16");
 }
 
+// One instantiation of the real unpack: 16-byte pairs when `pairs`.
+template <class R, int A, int B, bool RD>
+void launch_unpack_one(dim3 g, dim3 g2, bool pairs, cudaStream_t st, int64_t rows, int64_t cols, R alpha,
+                       ScaleMode<R> am, const R* src, int64_t lds, R beta, ScaleMode<R> bm, R* dst, int64_t ldd) {
+    if constexpr (sizeof(R) == 8) {
+        if (pairs) {
+            unpack_real2_kernel<A, B, RD><<<g2, 256, 0, st>>>(rows / 2, cols, alpha, am, (const double2*)src, lds / 2,
+                                                              beta, bm, (double2*)dst, ldd / 2);
+            return;
+        }
+    }
+    unpack_real_kernel<R, A, B, RD><<<g, 256, 0, st>>>(rows, cols, alpha, am, src, lds, beta, bm, dst, ldd);
+}
+
 // The real unpack for the scale modes of alpha and beta (beta's only when C
-// is read).
+// is read); 16-byte pairs of doubles where the layout allows.
 template <class R>
 void launch_unpack_real(dim3 g, cudaStream_t st, int64_t rows, int64_t cols, R alpha, ScaleMode<R> am, const R* src,
                         int64_t lds, R beta, ScaleMode<R> bm, R* dst, int64_t ldd, bool read_dst) {
+    const bool pairs = sizeof(R) == 8 && rows % 2 == 0 && lds % 2 == 0 && ldd % 2 == 0 &&
+                       ((uintptr_t)src | (uintptr_t)dst) % 16 == 0;
+    const dim3 g2 = grid2d(ceil_div(rows / 2, 4), cols, 256);
 #define CGB_UNPACK(A, B, RD) \
-    unpack_real_kernel<R, A, B, RD><<<g, 256, 0, st>>>(rows, cols, alpha, am.e, src, lds, beta, bm.e, dst, ldd)
+    launch_unpack_one<R, A, B, RD>(g, g2, pairs, st, rows, cols, alpha, am, src, lds, beta, bm, dst, ldd)
 #define CGB_UNPACK_B(A)                              \
     if (!read_dst) CGB_UNPACK(A, 0, false);          \
     else if (bm.mode == 0) CGB_UNPACK(A, 0, true);   \
     else if (bm.mode == 1) CGB_UNPACK(A, 1, true);   \
+    else if (bm.mode == 3) CGB_UNPACK(A, 3, true);   \
     else CGB_UNPACK(A, 2, true);
     if (am.mode == 0) { CGB_UNPACK_B(0) }
     else if (am.mode == 1) { CGB_UNPACK_B(1) }
+    else if (am.mode == 3) { CGB_UNPACK_B(3) }
     else { CGB_UNPACK_B(2) }
 #undef CGB_UNPACK_B
 #undef CGB_UNPACK

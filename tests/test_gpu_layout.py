@@ -30,12 +30,13 @@ def test_pack_bit_exact(native_lib, cuda, rows, cols, op, dtype):
 
 @pytest.mark.parametrize("alpha,beta", [(1.5, 0.5), (1.0, 0.0), (0.5, 1.0), (-2.0, -0.25), (1.0, 0.3), (0.5, 0.0),
                                         (-0.7, 1.0)])
-def test_unpack_real_bit_exact(native_lib, cuda, alpha, beta):
+@pytest.mark.parametrize("rows,ldd_extra", [(129, 7), (128, 8)])  # element-wise, and 16-byte pairs
+def test_unpack_real_bit_exact(native_lib, cuda, alpha, beta, rows, ldd_extra):
     from cosma_gb300 import unpack
-    rows, cols = 129, 77
+    cols = 77
     S = oracle.normal((rows, cols), 1)
     D0 = oracle.normal((rows, cols), 2)
-    ldd = rows + 7
+    ldd = rows + ldd_extra
     dS = to_dev(S)
     dD = to_dev(D0, ldd, fill=np.nan if beta == 0 else None)
     unpack(rows, cols, alpha, dS, rows, beta, dD, ldd, scalar="d")
@@ -44,11 +45,15 @@ def test_unpack_real_bit_exact(native_lib, cuda, alpha, beta):
     assert got.tobytes() == ref.tobytes()
 
 
-@pytest.mark.parametrize("alpha,beta", [(2.0, 0.5), (0.25, 4.0), (1.0, 2.0 ** -1000), (2.0 ** 1000, 1.0)])
+@pytest.mark.parametrize("alpha,beta", [(2.0, 0.5), (0.25, 4.0), (1.0, 2.0 ** -1000), (2.0 ** 1000, 1.0),
+                                        (1.5, 0.5), (-3.0, 0.75), (1.0 + 2.0 ** -10, -2047.0), (1.5 * 2.0 ** 900, 1.0),
+                                        (0.75 * 2.0 ** -1000, -1.5)])
 def test_unpack_power_of_two_scales_at_the_range_edges(native_lib, cuda, alpha, beta):
-    """Power-of-two alpha / beta scale by moving the exponent field; values whose
-    scaled exponent leaves the normal range (subnormals, overflow to Inf, the
-    smallest normals) must still round exactly as the FP64 multiply does."""
+    """Power-of-two alpha / beta scale by moving the exponent field, and scales
+    with a significand of at most 11 bits (1.5, -3, 0.75, 1 + 2^-10, -2047)
+    multiply in integer arithmetic; values whose product leaves the normal
+    range (subnormals, overflow to Inf, the smallest normals), zeros of both
+    signs and Inf / NaN must still round exactly as the FP64 multiply does."""
     from cosma_gb300 import unpack
     rows, cols = 64, 9
     rng = np.random.default_rng(9)
