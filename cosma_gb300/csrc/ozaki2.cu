@@ -1094,8 +1094,8 @@ Stats merge_stats(const Stats* s, const std::vector<int>& idx) {
     return r;
 }
 
-int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
-                         cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
+int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+                              cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
     *taken = false;
     const int64_t m = g.m, n = g.n, k = g.k;
     if (g.scalar != Scalar::D || k > KMAX || k < 1 || m < 1 || n < 1) return COSMA_GPU_SUCCESS;
@@ -1295,7 +1295,9 @@ int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaS
     if (full.nmod != N || full.P != pl.P) return abandon();
     full.exact = full.P >= exact_bits;
 
-    // 4. blocks in order; block b's C leaves on ds while block b+1 computes
+    // 4. blocks in order; block b's C leaves on ds while block b+1 computes.
+    // From here the call owns C: an error is the caller's, not a fall-back.
+    *taken = true;
     CombineParams cp0;
     fill_combine(cp0, N, pl.P);
     cudaEvent_t ev_comb[2] = {next_event(), next_event()}, ev_out[2] = {next_event(), next_event()},
@@ -1344,7 +1346,6 @@ int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaS
         }
         if (b + 2 < NBLK) CGB_CHECK(gemm_block(b + 2));  // after this block's reconstruction freed its R
     }
-    *taken = true;
     for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));
     CGB_CUDA(cudaMemcpy(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (*w->host_err)
@@ -1359,6 +1360,20 @@ int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaS
         info->spread_bits = full.spread;
     }
     return COSMA_GPU_SUCCESS;
+}
+
+// The overlapped form with its error exit: whatever fails, nothing is left in
+// flight on its streams when it returns.
+int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+                         cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
+    const int st = dgemm_host_pipelined_body(g, nmod_req, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
+    if (st != COSMA_GPU_SUCCESS) {
+        PipeWorkspace* w = pipe_workspace(cs);
+        for (cudaStream_t s : {cs, hs, ds, w->ss})
+            if (s) cudaStreamSynchronize(s);
+        cudaGetLastError();
+    }
+    return st;
 }
 
 }  // namespace oz2

@@ -247,9 +247,13 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
         int64_t h2d = 0, d2h = 0;
         bool taken = false;
         const size_t S = h->streams.size();
-        CGB_CHECK(ozaki2_dgemm_host(g, h->slices, h->streams[0], h->streams[1], h->streams[std::min<size_t>(2, S - 1)],
-                                    &oi, &h2d, &d2h, &taken));
-        if (taken) {
+        const int st = ozaki2_dgemm_host(g, h->slices, h->streams[0], h->streams[1],
+                                         h->streams[std::min<size_t>(2, S - 1)], &oi, &h2d, &d2h, &taken);
+        // a refused allocation before C is touched: the one-step form below
+        // needs less memory
+        if (st != COSMA_GPU_SUCCESS && (taken || st != COSMA_GPU_ERROR_OUT_OF_MEMORY)) return st;
+        if (st != COSMA_GPU_SUCCESS) clear_error();
+        if (taken && st == COSMA_GPU_SUCCESS) {
             *info = oi;
             h->last_h2d_bytes = h2d;
             h->last_d2h_bytes = d2h;

@@ -127,3 +127,40 @@ def test_failed_staging_allocation_falls_back_to_driver_copies(native_lib, cuda,
     np.testing.assert_array_equal(got, ref)
     if not consumed:
         pytest.skip("the process-wide staging buffers already existed: no allocation was attempted")
+
+
+def test_overlapped_form_allocation_failure_falls_back(native_lib, cuda, monkeypatch):
+    """A refused device allocation inside the overlapped one-step form
+    (page-locked host operands, Chinese-remainder method), before it touches
+    C, gives way to the regular one-step path: the same bits as with the
+    overlap switched off, and the handle stays usable."""
+    import torch
+
+    import cosma_gb300 as cg
+    m, n, k = 2100, 2300, 300
+    A, B = oracle.uniform((m, k), 91), oracle.uniform((k, n), 92)
+    pin = lambda X: torch.from_numpy(np.ascontiguousarray(X.T).reshape(-1)).pin_memory()
+    hA, hB = pin(A), pin(B)
+
+    def run(h):
+        hC = torch.zeros(m * n, dtype=torch.float64).pin_memory()
+        cg.gemm(h, "N", "N", m, n, k, 1.0, hA, m, hB, k, 0.0, hC, m)
+        return hC.numpy().copy(), h.ozaki_info()
+
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "OFF")
+    h = cg.make_context("d", 2)
+    h.set_method("ozaki2", 0)
+    want, _ = run(h)
+    h.close()
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "ON")
+    h = cg.make_context("d", 2)  # fresh streams: the overlapped form allocates its buffers now
+    h.set_method("ozaki2", 0)
+    native_lib.cosma_gpu_test_fail_next(DEVICE_ALLOC, 1)
+    got, info = run(h)
+    assert native_lib.cosma_gpu_test_faults_pending(DEVICE_ALLOC) == 0
+    assert info["gemm_ms"] > 0.0  # the regular one-step path ran (the overlapped form times no phases)
+    np.testing.assert_array_equal(got, want)
+    again, info = run(h)  # the next call takes the overlapped form
+    assert info["gemm_ms"] == 0.0
+    np.testing.assert_array_equal(again, want)
+    h.close()
