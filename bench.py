@@ -326,6 +326,7 @@ def cfg_pdgemm(steps, warmup):
         t0 = time.perf_counter()
         cg.pxgemm("T", "N", m, n, k, alpha, A, 1, 1, desca, B, 1, 1, descb, beta, Ch, 1, 1, descc)
         e2e.append(time.perf_counter() - t0)
+    h2d_px, d2h_px, overlapped = cg.pxgemm_last_transfers()
     cg.pxgemm_set_method("native")
     e2e_s = float(np.median(e2e))
     # accuracy of the host result on sampled entries (double-double oracle)
@@ -358,9 +359,13 @@ def cfg_pdgemm(steps, warmup):
                          "pack_B_frac": gbs(pack_b_bytes, t[1]) / pk["hbm_gbs"]},
             "accuracy": {"max_rel_err": float(rel.max()), "mean_rel_err": float(rel.mean()), "samples": 1024,
                          "reference": "double-double (oracle) on sampled entries"},
-            "e2e": {"value": flops / e2e_s / 1e12, "unit": UNIT, "h2d_bytes_per_step": (m * k + k * n + m * n) * 8,
-                    "d2h_bytes_per_step": m * n * 8, "entry": "pdgemm_ (ScaLAPACK symbol), host arrays",
-                    "host_copy_route": cg.host_copy_route(A), "ms_per_step": e2e_s * 1e3},
+            "e2e": {"value": flops / e2e_s / 1e12, "unit": UNIT, "h2d_bytes_per_step": h2d_px,
+                    "d2h_bytes_per_step": d2h_px, "entry": "pdgemm_ (ScaLAPACK symbol), pageable host arrays",
+                    "form": ("overlapped one-step: op(A) / op(B) panels and C blocks on the copy engines, issued "
+                             "by a copy thread, beside the modular GEMMs") if overlapped else
+                            "staged: whole arrays copied in, pack, GEMM, unpack, C copied out",
+                    "host_copy_route": cg.host_copy_route(A), "ms_per_step": e2e_s * 1e3,
+                    "calls_ms": [round(x * 1e3, 2) for x in e2e]},
             "cpu_baseline": {"value": 2.0 * m * n * kb / cpu_s / 1e12, "unit": UNIT, "cores": oracle.openblas_threads(),
                              "kind": "port",
                              "sample": f"numpy pack of A^T, OpenBLAS DGEMM {m}x{n}x{kb} K-slab, alpha/beta ({cpu_s:.1f} s)"},

@@ -7,7 +7,8 @@ from ._native import (CosmaGpuError, METHOD_AUTO, METHOD_BF16X3, METHOD_NATIVE, 
                       LIB_PATH, load)
 from .api import (BlockLayout, GroupedPlan, MMHandle, dgemm_ozaki_device, dgemm_ozaki2_device,  # noqa: F401
                   multiply_using_layout, descinit, gemm, gemm_device, host_copy_route, local_multiply, make_context,
-                  dgemm_ozaki2_residual, ozaki2_choose, pack, pxgemm, pxgemm_set_method, release_workspaces,
+                  dgemm_ozaki2_residual, ozaki2_choose, pack, pxgemm, pxgemm_last_transfers, pxgemm_set_method,
+                  release_workspaces,
                   tiles_for_memory, unpack, zgemm_ozaki_device,
                   zgemm_ozaki2_device)
 

@@ -122,6 +122,7 @@ SIGNATURES = {
     "costa_gpu_unpack_z": (i32, [i64, i64, vp, vp, i64, vp, vp, i64, vp]),
     "costa_gpu_unpack_c": (i32, [i64, i64, vp, vp, i64, vp, vp, i64, vp]),
     "cosma_gpu_pxgemm_set_method": (i32, [i32]),
+    "cosma_gpu_pxgemm_last_transfers": (i32, [C.POINTER(i64), C.POINTER(i64), C.POINTER(C.c_int)]),
     "cosma_gpu_test_fail_next": (i32, [i32, i32]),
     "cosma_gpu_test_faults_pending": (i32, [i32]),
     "cosma_gpu_host_copy_route": (i32, [vp]),

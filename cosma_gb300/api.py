@@ -190,6 +190,15 @@ def pxgemm_set_method(method="native"):
     N.check(lib.cosma_gpu_pxgemm_set_method(N.METHODS[method] if isinstance(method, str) else int(method)))
 
 
+def pxgemm_last_transfers():
+    """(h2d_bytes, d2h_bytes, overlapped) of the last p?gemm call: the bytes
+    its host arrays moved, and whether the overlapped one-step form ran it."""
+    lib = N.load()
+    h2d, d2h, ov = C.c_int64(0), C.c_int64(0), C.c_int(0)
+    N.check(lib.cosma_gpu_pxgemm_last_transfers(C.byref(h2d), C.byref(d2h), C.byref(ov)))
+    return h2d.value, d2h.value, bool(ov.value)
+
+
 HOST_COPY_ROUTES = {0: "memcpy", 1: "staged", 2: "direct"}
 
 

@@ -54,8 +54,13 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace cgb {
@@ -1000,6 +1005,85 @@ int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
 }
 
 // ------------------------------------------------------ host operands, overlapped
+// Host copies issued from a worker thread, in order.  A copy of pageable
+// host memory returns only once it is done (even cudaMemcpy2DAsync), so the
+// thread that feeds the GPU must not issue it; page-locked copies return at
+// once either way.  post() queues a task and returns its ticket; wait(t)
+// returns once task t has run (its copy issued, or for pageable memory done,
+// and its event recorded), with the first error of the tasks so far.
+class CopyWorker {
+public:
+    explicit CopyWorker(int device) : device_(device), th_([this] { loop(); }) {}
+    ~CopyWorker() {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        th_.join();
+    }
+    uint64_t post(std::function<int()> task) {
+        std::lock_guard<std::mutex> lock(mu_);
+        q_.push_back(std::move(task));
+        cv_.notify_all();
+        return ++posted_;
+    }
+    // An error of the worker's thread is reported again on the caller's (the
+    // library's last-error record is per thread).
+    int wait(uint64_t ticket) {
+        std::unique_lock<std::mutex> lock(mu_);
+        cv_.wait(lock, [&] { return done_ >= ticket; });
+        if (err_ != COSMA_GPU_SUCCESS) set_error(err_, msg_);
+        return err_;
+    }
+    int drain() {
+        uint64_t t;
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            t = posted_;
+        }
+        const int e = wait(t);
+        std::lock_guard<std::mutex> lock(mu_);
+        err_ = COSMA_GPU_SUCCESS;  // reported once
+        msg_.clear();
+        return e;
+    }
+
+private:
+    void loop() {
+        cudaSetDevice(device_);
+        for (;;) {
+            std::function<int()> task;
+            {
+                std::unique_lock<std::mutex> lock(mu_);
+                cv_.wait(lock, [&] { return stop_ || !q_.empty(); });
+                if (q_.empty()) return;  // stopping
+                task = std::move(q_.front());
+                q_.pop_front();
+            }
+            const int e = task();
+            {
+                std::lock_guard<std::mutex> lock(mu_);
+                if (e != COSMA_GPU_SUCCESS && err_ == COSMA_GPU_SUCCESS) {
+                    err_ = e;
+                    msg_ = std::string("overlapped host copy: ") + cosma_gpu_last_error_string();
+                }
+                ++done_;
+            }
+            cv_.notify_all();
+        }
+    }
+    int device_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<std::function<int()>> q_;
+    uint64_t posted_ = 0, done_ = 0;
+    int err_ = COSMA_GPU_SUCCESS;
+    std::string msg_;
+    bool stop_ = false;
+    std::thread th_;  // last: started once everything it uses exists
+};
+
 // One-step DGEMM on host A, B and C (C = alpha op(A) op(B) + beta C), with the
 // host link's copies overlapped with the work: op(A) arrives in MA row panels
 // and op(B) in NB column panels on the copy stream, each panel's exponents
@@ -1016,6 +1100,7 @@ struct PipeWorkspace {
     unsigned* host_err = nullptr;
     std::vector<cudaEvent_t> ev;
     cudaStream_t ss = nullptr;  // exponents and statistics of landed panels, beside the GEMMs
+    std::unique_ptr<CopyWorker> worker;
 };
 
 std::mutex g_pipe_mu;
@@ -1038,6 +1123,13 @@ PipeWorkspace* pipe_workspace(cudaStream_t s) {
             if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) e = nullptr;
     }
     if (!w->ss && cudaStreamCreateWithFlags(&w->ss, cudaStreamNonBlocking) != cudaSuccess) w->ss = nullptr;
+    if (!w->worker) {
+        try {
+            w->worker.reset(new CopyWorker(dev));
+        } catch (...) {  // no thread to be had: the overlapped form is not taken
+            w->worker.reset();
+        }
+    }
     cudaGetLastError();
     return w;
 }
@@ -1053,6 +1145,7 @@ void release_pipe_workspace(cudaStream_t s) {
         w = it->second;
         g_pipe.erase(it);
     }
+    w->worker.reset();  // runs what is queued (copies recording the events below), then joins
     if (w->host_stats) cudaFreeHost(w->host_stats);
     if (w->host_err) cudaFreeHost(w->host_err);
     for (auto e : w->ev)
@@ -1109,6 +1202,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     for (auto e : w->ev)
         if (!e) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: pipeline events");
     if (!w->ss) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: pipeline stream");
+    if (!w->worker) return COSMA_GPU_SUCCESS;  // no copy thread: the regular path
     cudaStream_t ss = w->ss;
     const int64_t k_pad = ceil_div(k, BKE) * BKE;
     const double* A = (const double*)g.A;
@@ -1155,31 +1249,44 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     *h2d_bytes = 0;
     *d2h_bytes = 0;
 
+    // Host copies go through the copy engines (copy kernels would take SM room
+    // the persistent GEMMs wait for), issued by the copy worker.
+    CopyWorker& cw = *w->worker;
+    auto copy_task = [](void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                        cudaMemcpyKind kind, cudaStream_t st, cudaEvent_t wait_ev, cudaEvent_t done_ev) {
+        return [=]() -> int {
+            if (wait_ev) CGB_CUDA(cudaStreamWaitEvent(st, wait_ev, 0));
+            CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, st));
+            CGB_CUDA(cudaEventRecord(done_ev, st));
+            return COSMA_GPU_SUCCESS;
+        };
+    };
+    uint64_t tk_copy[kPipeMaxPanels] = {};
     // device copy of op(A) rows / op(B) columns of one panel, compact
     auto copy_panel = [&](int p) -> int {
+        ev_copy[p] = next_event();
         if (p < MA) {
             const int64_t i0 = PA.first(p), mi = PA.rows(p, m);
-            if (!a_kc) CGB_CHECK(copy_2d_overlapped(dA + offA[p], mi * 8, A + i0, g.lda * 8, mi * 8, k,
-                                                    cudaMemcpyHostToDevice, hs));
-            else CGB_CHECK(copy_2d_overlapped(dA + offA[p], k * 8, A + i0 * g.lda, g.lda * 8, k * 8, mi,
-                                              cudaMemcpyHostToDevice, hs));
+            if (!a_kc) tk_copy[p] = cw.post(copy_task(dA + offA[p], mi * 8, A + i0, g.lda * 8, mi * 8, k,
+                                                      cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
+            else tk_copy[p] = cw.post(copy_task(dA + offA[p], k * 8, A + i0 * g.lda, g.lda * 8, k * 8, mi,
+                                                cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
             *h2d_bytes += mi * k * 8;
         } else {
             const int j = p - MA;
             const int64_t j0 = PB.first(j), nj = PB.rows(j, n);
-            if (b_kc) CGB_CHECK(copy_2d_overlapped(dB + offB[j], k * 8, B + j0 * g.ldb, g.ldb * 8, k * 8, nj,
-                                                   cudaMemcpyHostToDevice, hs));
-            else CGB_CHECK(copy_2d_overlapped(dB + offB[j], nj * 8, B + j0, g.ldb * 8, nj * 8, k,
-                                              cudaMemcpyHostToDevice, hs));
+            if (b_kc) tk_copy[p] = cw.post(copy_task(dB + offB[j], k * 8, B + j0 * g.ldb, g.ldb * 8, k * 8, nj,
+                                                     cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
+            else tk_copy[p] = cw.post(copy_task(dB + offB[j], nj * 8, B + j0, g.ldb * 8, nj * 8, k,
+                                                cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
             *h2d_bytes += nj * k * 8;
         }
-        ev_copy[p] = next_event();
-        CGB_CUDA(cudaEventRecord(ev_copy[p], hs));
         return COSMA_GPU_SUCCESS;
     };
     // exponents and statistics of one panel as soon as it lands, on the
     // statistics stream (small kernels that run beside the GEMMs)
     auto scale_panel = [&](int p) -> int {
+        CGB_CHECK(cw.wait(tk_copy[p]));  // its event is recorded
         CGB_CUDA(cudaStreamWaitEvent(ss, ev_copy[p], 0));
         if (p < MA) {
             const int64_t mi = PA.rows(p, m);
@@ -1195,8 +1302,9 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         CGB_CUDA(cudaEventRecord(ev_scaled[p], ss));
         return COSMA_GPU_SUCCESS;
     };
-    // drains every stream (the caller then runs the regular path)
+    // drains the copy worker and every stream (the caller then runs the regular path)
     auto abandon = [&]() -> int {
+        CGB_CHECK(cw.drain());
         for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));
         *h2d_bytes = 0;
         return COSMA_GPU_SUCCESS;
@@ -1228,15 +1336,18 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     CGB_CHECK(w->resB.reserve((size_t)rb * 2, cs));
     for (auto& r : w->R) CGB_CHECK(r.reserve((size_t)N * ma_pad * nb_pad, cs));
 
-    // 2. the other panels: B's first (block row 0 uses them), then A's; each
-    // is scaled as it lands
-    for (int p = MA + 1; p < NP; ++p) CGB_CHECK(copy_panel(p));
-    for (int p = 1; p < MA; ++p) CGB_CHECK(copy_panel(p));
-    for (int p = MA + 1; p < NP; ++p) CGB_CHECK(scale_panel(p));
-    for (int p = 1; p < MA; ++p) CGB_CHECK(scale_panel(p));
-    cudaEvent_t ev_stats = next_event();
-    CGB_CUDA(cudaMemcpyAsync(w->host_stats, sdev, (size_t)NP * sizeof(Stats), cudaMemcpyDeviceToHost, ss));
-    CGB_CUDA(cudaEventRecord(ev_stats, ss));
+    // 2. the other panels: B's first (block row 0 uses them), then A's
+    std::vector<int> order;
+    for (int p = MA + 1; p < NP; ++p) order.push_back(p);
+    for (int p = 1; p < MA; ++p) order.push_back(p);
+    for (int p : order) CGB_CHECK(copy_panel(p));
+    std::vector<char> scaled(NP, 0);
+    scaled[0] = scaled[MA] = 1;
+    auto ensure_scaled = [&](int p) -> int {
+        if (scaled[p]) return COSMA_GPU_SUCCESS;
+        scaled[p] = 1;
+        return scale_panel(p);
+    };
 
     SplitParams sp;
     fill_split(sp, N, pl.P);
@@ -1274,10 +1385,19 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     };
 
     // 3. the first two blocks start while the other panels are on the way
-    // (two, so that a slow link leaves the GPU work until the last panel is in)
+    // (two, so that a slow link leaves the GPU work until the last panel is
+    // in); every other panel is scaled as it lands.  A panel's scale kernels
+    // are issued once its copy task has run (for pageable memory, once the
+    // copy itself is done), so block 0 is launched first.
     const int NBLK = MA * NB;
     CGB_CHECK(gemm_block(0));
+    CGB_CHECK(ensure_scaled(1 / NB));
+    CGB_CHECK(ensure_scaled(MA + (1 % NB)));
     CGB_CHECK(gemm_block(1));
+    for (int p : order) CGB_CHECK(ensure_scaled(p));
+    cudaEvent_t ev_stats = next_event();
+    CGB_CUDA(cudaMemcpyAsync(w->host_stats, sdev, (size_t)NP * sizeof(Stats), cudaMemcpyDeviceToHost, ss));
+    CGB_CUDA(cudaEventRecord(ev_stats, ss));
     // every panel's statistics, then the check that the first panels chose
     // the modulus count the whole data gives
     CGB_CUDA(cudaEventSynchronize(ev_stats));
@@ -1303,6 +1423,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     cudaEvent_t ev_comb[2] = {next_event(), next_event()}, ev_out[2] = {next_event(), next_event()},
                 ev_cin[2] = {next_event(), next_event()};
     bool out_used[2] = {false, false};
+    uint64_t tk_out[2] = {0, 0};  // the copy-out of each C slot
     for (int b = 0; b < NBLK; ++b) {
         {
             const int i = b / NB, j = b % NB;
@@ -1310,13 +1431,14 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             const int slot = b & 1;
             double* cdev = (double*)w->C[slot].ptr;
             if (!beta_zero) {  // the old C block comes in once its slot has been drained
-                if (out_used[slot]) CGB_CUDA(cudaStreamWaitEvent(hs, ev_out[slot], 0));
-                CGB_CHECK(copy_2d_overlapped(cdev, mi * 8, C + i0 + j0 * g.ldc, g.ldc * 8, mi * 8, nj,
-                                             cudaMemcpyHostToDevice, hs));
+                const uint64_t t = cw.post(copy_task(cdev, mi * 8, C + i0 + j0 * g.ldc, g.ldc * 8, mi * 8, nj,
+                                                     cudaMemcpyHostToDevice, hs, out_used[slot] ? ev_out[slot] : nullptr,
+                                                     ev_cin[slot]));
                 *h2d_bytes += mi * nj * 8;
-                CGB_CUDA(cudaEventRecord(ev_cin[slot], hs));
+                CGB_CHECK(cw.wait(t));
                 CGB_CUDA(cudaStreamWaitEvent(cs, ev_cin[slot], 0));
             } else if (out_used[slot]) {
+                CGB_CHECK(cw.wait(tk_out[slot]));
                 CGB_CUDA(cudaStreamWaitEvent(cs, ev_out[slot], 0));
             }
             CombineParams cp = cp0;
@@ -1337,15 +1459,14 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             cp.beta_zero = beta_zero;
             CGB_CHECK(launch_combine(cp, N, nj, cs));
             CGB_CUDA(cudaEventRecord(ev_comb[slot], cs));
-            CGB_CUDA(cudaStreamWaitEvent(ds, ev_comb[slot], 0));
-            CGB_CHECK(copy_2d_overlapped(C + i0 + j0 * g.ldc, g.ldc * 8, cdev, mi * 8, mi * 8, nj,
-                                         cudaMemcpyDeviceToHost, ds));
+            tk_out[slot] = cw.post(copy_task(C + i0 + j0 * g.ldc, g.ldc * 8, cdev, mi * 8, mi * 8, nj,
+                                             cudaMemcpyDeviceToHost, ds, ev_comb[slot], ev_out[slot]));
             *d2h_bytes += mi * nj * 8;
-            CGB_CUDA(cudaEventRecord(ev_out[slot], ds));
             out_used[slot] = true;
         }
         if (b + 2 < NBLK) CGB_CHECK(gemm_block(b + 2));  // after this block's reconstruction freed its R
     }
+    CGB_CHECK(cw.drain());
     for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));
     CGB_CUDA(cudaMemcpy(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost));
     if (*w->host_err)
@@ -1369,6 +1490,7 @@ int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaS
     const int st = dgemm_host_pipelined_body(g, nmod_req, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
     if (st != COSMA_GPU_SUCCESS) {
         PipeWorkspace* w = pipe_workspace(cs);
+        if (w->worker) w->worker->drain();
         for (cudaStream_t s : {cs, hs, ds, w->ss})
             if (s) cudaStreamSynchronize(s);
         cudaGetLastError();

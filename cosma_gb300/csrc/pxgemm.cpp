@@ -33,7 +33,11 @@ namespace {
 std::mutex g_px_mu;
 int g_px_method = -1;
 cudaStream_t g_px_stream = nullptr;
+cudaStream_t g_px_copy[2] = {nullptr, nullptr};  // host-to-device, device-to-host (the overlapped form)
 DeviceBuffer g_px_buf[6];  // A_sc, A_cosma, B_sc, B_cosma, C_cosma, C_sc
+// the last call's host<->HBM bytes and whether the overlapped form ran it
+int64_t g_px_h2d = 0, g_px_d2h = 0;
+int g_px_overlapped = 0;
 
 int px_method() {
     if (g_px_method < 0) g_px_method = default_method();
@@ -86,8 +90,10 @@ int stage_in(const void* p, int64_t rows, int64_t cols, int64_t ld, size_t es, D
     CGB_CHECK(buf.reserve(std::max<size_t>((size_t)rows * cols * es, 16), s));
     *dptr = buf.ptr;
     *dld = std::max<int64_t>(rows, 1);
-    if (copy && rows > 0 && cols > 0)
+    if (copy && rows > 0 && cols > 0) {
         CGB_CHECK(copy_h2d_2d(buf.ptr, (size_t)*dld * es, p, (size_t)ld * es, (size_t)rows * es, (size_t)cols, s));
+        g_px_h2d += rows * cols * (int64_t)es;
+    }
     return COSMA_GPU_SUCCESS;
 }
 
@@ -112,6 +118,8 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
     char* csub = (char*)c + ((int64_t)(*pic - 1) + (int64_t)(*pjc - 1) * lldc) * es;
 
     std::lock_guard<std::mutex> lock(g_px_mu);
+    g_px_h2d = g_px_d2h = 0;
+    g_px_overlapped = 0;
     if (!g_px_stream) CGB_CUDA(cudaStreamCreateWithFlags(&g_px_stream, cudaStreamNonBlocking));
     cudaStream_t s = g_px_stream;
     const bool c_dev = is_dev(c);
@@ -124,7 +132,10 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
         int64_t ldC;
         CGB_CHECK(stage_in(csub, m, n, lldc, es, g_px_buf[5], !beta_zero, &dC, &ldC, s));
         CGB_CHECK(scale_matrix_device(sc, m, n, beta, (void*)dC, ldC, s));
-        if (!c_dev) CGB_CHECK(copy_d2h_2d(csub, lldc * es, dC, ldC * es, (size_t)m * es, n, s));
+        if (!c_dev) {
+            CGB_CHECK(copy_d2h_2d(csub, lldc * es, dC, ldC * es, (size_t)m * es, n, s));
+            g_px_d2h = (int64_t)m * n * (int64_t)es;
+        }
         CGB_CUDA(cudaStreamSynchronize(s));
         return COSMA_GPU_SUCCESS;
     }
@@ -139,6 +150,32 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
     const int64_t llda = desca[8], lldb = descb[8];
     const char* asub = (const char*)a + ((int64_t)(*pia - 1) + (int64_t)(*pja - 1) * llda) * es;
     const char* bsub = (const char*)b + ((int64_t)(*pib - 1) + (int64_t)(*pjb - 1) * lldb) * es;
+
+    // Host A, B and C of a real double problem under the Chinese-remainder
+    // method: the overlapped one-step form copies op(A) row panels and op(B)
+    // column panels straight from the ScaLAPACK buffers while earlier blocks
+    // compute and sends C blocks back while later ones do.  Its reconstruction
+    // rounds fl(fl(alpha * fl(A B)) + fl(beta * C)), which is steps 3 and 4
+    // below to the bit (the product rounded once, then the unpack's scaling).
+    // When its first panels would choose another modulus count than the whole
+    // data, or the data holds Inf/NaN, or a buffer is refused before C is
+    // touched, the staged path below runs.
+    if (sc == Scalar::D && px_method() == COSMA_GPU_METHOD_OZAKI2 && !c_dev && !is_dev(asub) && !is_dev(bsub) &&
+        env_bool("COSMA_GPU_OZAKI2_OVERLAP", true)) {
+        for (auto& cs : g_px_copy)
+            if (!cs) CGB_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        const GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, asub, llda, bsub, lldb, beta, csub, lldc);
+        int64_t h2d = 0, d2h = 0;
+        bool taken = false;
+        const int st = ozaki2_dgemm_host(g, 0, s, g_px_copy[0], g_px_copy[1], nullptr, &h2d, &d2h, &taken);
+        if (taken && st == COSMA_GPU_SUCCESS) {
+            g_px_h2d = h2d;
+            g_px_d2h = d2h;
+            g_px_overlapped = 1;
+        }
+        if (taken || (st != COSMA_GPU_SUCCESS && st != COSMA_GPU_ERROR_OUT_OF_MEMORY)) return st;
+        clear_error();
+    }
 
     // 1. stage the ScaLAPACK sub-matrices in HBM
     const void *dAsc, *dBsc, *dCsc;
@@ -163,7 +200,10 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
     CGB_CHECK(gemm_device(g, px_method(), 0, s, nullptr));
     // 4. C_sc = alpha * C_cosma + beta * C_sc
     CGB_CHECK(unpack_device(sc, m, n, alpha, dCc, m, beta, (void*)dCsc, ldCsc, s));
-    if (!c_dev) CGB_CHECK(copy_d2h_2d(csub, lldc * es, dCsc, ldCsc * es, (size_t)m * es, n, s));
+    if (!c_dev) {
+        CGB_CHECK(copy_d2h_2d(csub, lldc * es, dCsc, ldCsc * es, (size_t)m * es, n, s));
+        g_px_d2h = (int64_t)m * n * (int64_t)es;
+    }
     CGB_CUDA(cudaStreamSynchronize(s));
     return COSMA_GPU_SUCCESS;
 }
@@ -248,6 +288,14 @@ int cosma_gpu_pxgemm_set_method(int method) {
         return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "pxgemm_set_method: unknown method");
     std::lock_guard<std::mutex> lock(cgb::g_px_mu);
     cgb::g_px_method = method;
+    return COSMA_GPU_SUCCESS;
+}
+
+int cosma_gpu_pxgemm_last_transfers(int64_t* h2d_bytes, int64_t* d2h_bytes, int* overlapped) {
+    std::lock_guard<std::mutex> lock(cgb::g_px_mu);
+    if (h2d_bytes) *h2d_bytes = cgb::g_px_h2d;
+    if (d2h_bytes) *d2h_bytes = cgb::g_px_d2h;
+    if (overlapped) *overlapped = cgb::g_px_overlapped;
     return COSMA_GPU_SUCCESS;
 }
 

@@ -231,17 +231,18 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     const int64_t ntiles = ntm * ntn, nsteps = ntiles * ntk;
     const bool keep_on_device = !dC && !copy_c_back;
     const bool crt = h->method == COSMA_GPU_METHOD_OZAKI2 && (sc == Scalar::D || sc == Scalar::Z);
-    // One step on page-locked host operands with the Chinese-remainder
-    // method: the overlapped form (op(A) / op(B) panels copied by the copy
-    // engines while earlier blocks compute, C blocks copied out while later
-    // ones do) where it applies; 16384^3 took 99.5 to 101 ms per call in it
-    // against 116 ms in the one-step form.  Pageable arrays keep the one-step
-    // form: copy kernels beside the modular GEMM cost it as much as they save.
+    // One step on host operands with the Chinese-remainder method: the
+    // overlapped form (op(A) / op(B) panels copied by the copy engines while
+    // earlier blocks compute, C blocks copied out while later ones do) where
+    // it applies; 16384^3 from page-locked arrays took 99.5 to 101 ms per call
+    // in it against 116 ms in the one-step form.  Its copies are issued by a
+    // worker thread, so pageable arrays (whose copies return only once done)
+    // overlap too.
     const bool overlap = env_bool("COSMA_GPU_OZAKI2_OVERLAP", true);
     // With two streams the C blocks leave on the copy stream, behind every
     // panel copy (those end long before the first block is reconstructed).
     if (overlap && crt && sc == Scalar::D && !dA && !dB && !dC && !trivial && !keep_on_device && nsteps == 1 &&
-        h->streams.size() >= 2 && host_page_locked(A) && host_page_locked(B) && host_page_locked(C)) {
+        h->streams.size() >= 2) {
         const GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
         cosma_gpu_ozaki_info oi{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
         int64_t h2d = 0, d2h = 0;

@@ -474,9 +474,18 @@ void COSMA_PCGEMM_(COSMA_GPU_PXGEMM_ARGS(float));
 void COSMA_PZGEMM_(COSMA_GPU_PXGEMM_ARGS(double));
 
 /* Method used by the p?gemm entry points (default NATIVE; the
- * COSMA_GPU_GEMM_METHOD environment variable "native"/"ozaki"/"bf16x3"
- * sets the initial value). */
+ * COSMA_GPU_GEMM_METHOD environment variable "native"/"ozaki"/"bf16x3"/
+ * "ozaki2" sets the initial value).  With OZAKI2, a real double call on host
+ * A, B and C runs in the overlapped one-step form (panel copies, modular
+ * GEMMs and C copies overlapped; the same bits as the staged form) unless
+ * COSMA_GPU_OZAKI2_OVERLAP=OFF. */
 int cosma_gpu_pxgemm_set_method(int method);
+
+/* The last p?gemm call's host-to-device and device-to-host bytes (the
+ * copies of host arrays; 0 for device arrays) and whether the overlapped
+ * form ran it (1) or the staged one (0).
+ * New: a diagnostic of this library; the reference has no counterpart. */
+int cosma_gpu_pxgemm_last_transfers(int64_t* h2d_bytes, int64_t* d2h_bytes, int* overlapped);
 
 /* Route a host <-> HBM copy of the array at `ptr` takes inside the
  * host-pointer entry points (p?gemm, multiply_using_layout):

@@ -175,3 +175,53 @@ def test_host_direct_copies_odd_layouts(native_lib, cuda, monkeypatch):
         pxgemm("T", "N", m, n, k, 1.0, A, 2, 2, desca, B, 1, 3, descb, 0.5, Ch, 3, 2, descc)
         outs.append(Ch.tobytes())
     assert outs[0] == outs[1]
+
+
+@pytest.mark.parametrize("ta,beta", [("T", 0.5), ("N", 0.0), ("C", -1.0)])
+def test_overlapped_pdgemm_host_arrays(native_lib, cuda, monkeypatch, ta, beta):
+    """pdgemm_ on host (pageable numpy) arrays under the Chinese-remainder
+    method, large enough for the overlapped one-step form (2 x 2 panels):
+    bit-identical to the staged form (COSMA_GPU_OZAKI2_OVERLAP=OFF) and to the
+    same call on device arrays; C outside the sub-matrix untouched, and C not
+    read when beta == 0 (NaN there)."""
+    import torch
+    from cosma_gb300 import descinit, pxgemm, pxgemm_last_transfers, pxgemm_set_method
+    m, n, k = 2100, 2300, 300
+    am, an = (m, k) if ta == "N" else (k, m)
+    lda, ldb, ldc = am + 3, k + 1, m + 5
+    A = oracle.exp_spread((lda, an + 1), 91, 6)
+    B = oracle.exp_spread((ldb, n + 2), 92, 6)
+    C0 = oracle.uniform((ldc, n + 2), 93)
+    if beta == 0:
+        C0[2:2 + m, 1:1 + n] = np.nan
+    desca = descinit(lda, an + 1, 64, 64, 0, 0, 0, lda)
+    descb = descinit(ldb, n + 2, 64, 64, 0, 0, 0, ldb)
+    descc = descinit(ldc, n + 2, 64, 64, 0, 0, 0, ldc)
+    args = lambda a, b, c: (ta, "N", m, n, k, 0.75, a, 2, 2, desca, b, 2, 3, descb, beta, c, 3, 2, descc)
+    pxgemm_set_method("ozaki2")
+    try:
+        outs = {}
+        for mode in ("ON", "OFF"):
+            monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", mode)
+            Ch = C0.copy(order="F")
+            pxgemm(*args(np.asfortranarray(A), np.asfortranarray(B), Ch))
+            outs[mode] = (Ch, pxgemm_last_transfers())
+        dA = torch.from_numpy(A.reshape(-1, order="F").copy()).cuda()
+        dB = torch.from_numpy(B.reshape(-1, order="F").copy()).cuda()
+        dC = torch.from_numpy(C0.reshape(-1, order="F").copy()).cuda()
+        pxgemm(*args(dA, dB, dC), scalar="d")
+        dev_moved = pxgemm_last_transfers()
+    finally:
+        pxgemm_set_method("native")
+    on, (h2d, d2h, overlapped) = outs["ON"]
+    off, (h2d_off, d2h_off, overlapped_off) = outs["OFF"]
+    assert overlapped and not overlapped_off
+    assert on.tobytes() == off.tobytes()
+    assert on.tobytes() == np.asfortranarray(dC.cpu().numpy().reshape(n + 2, ldc).T).tobytes()
+    mask = np.ones(on.shape, bool)
+    mask[2:2 + m, 1:1 + n] = False
+    assert on[mask].tobytes() == C0[mask].tobytes()
+    assert not np.isnan(on[2:2 + m, 1:1 + n]).any()
+    moved = 8 * (m * k + k * n + (m * n if beta != 0 else 0))
+    assert (h2d, d2h) == (moved, 8 * m * n) == (h2d_off, d2h_off)
+    assert dev_moved == (0, 0, False)
