@@ -16,7 +16,10 @@
 #include "runtime.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <unistd.h>
@@ -63,27 +66,112 @@ int copy_threads() {
     return n;
 }
 
+// Host threads kept for the parallel copies below: run(nt, f) calls f(t)
+// for t = 0 .. nt-1, f(0) on the calling thread, and returns when all are
+// done.  One job at a time; starting threads per job cost ~0.3 ms per
+// 128 MB staging chunk.  A pool that cannot start its threads runs the job
+// on the calling thread alone.
+class HostPool {
+   public:
+    void run(int nt, const std::function<void(int)>& f) {
+        std::lock_guard<std::mutex> job(job_mu_);
+        if (nt > 1 && !start(nt - 1)) nt = 1;
+        if (nt == 1) {
+            f(0);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            fn_ = &f;
+            parts_ = nt;
+            left_ = nt - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        f(0);
+        std::unique_lock<std::mutex> lock(mu_);
+        done_cv_.wait(lock, [&] { return left_ == 0; });
+        fn_ = nullptr;
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lock(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& t : th_) t.join();
+    }
+
+   private:
+    bool start(int want) {
+        try {
+            while ((int)th_.size() < want) {
+                const int id = (int)th_.size() + 1;
+                th_.emplace_back([this, id] { loop(id); });
+            }
+        } catch (...) {
+            return false;  // joined threads stay; this job runs alone
+        }
+        return true;
+    }
+    void loop(int id) {
+        unsigned long long seen = 0;
+        for (;;) {
+            const std::function<void(int)>* f;
+            {
+                std::unique_lock<std::mutex> lock(mu_);
+                cv_.wait(lock, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                if (id >= parts_) continue;  // not part of this job
+                f = fn_;
+            }
+            (*f)(id);
+            {
+                std::lock_guard<std::mutex> lock(mu_);
+                if (--left_ == 0) done_cv_.notify_all();
+            }
+        }
+    }
+    std::mutex job_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    std::vector<std::thread> th_;
+    const std::function<void(int)>* fn_ = nullptr;
+    int parts_ = 0, left_ = 0;
+    unsigned long long gen_ = 0;
+    bool stop_ = false;
+};
+
+HostPool& host_pool() {
+    static HostPool* pool = new HostPool();  // never destroyed: threads may outlive static destruction order
+    return *pool;
+}
+
+// Runs body(c0, c1) over [0, cols) in pieces of about `bytes_per_piece`
+// bytes (`width` bytes a column) on nt threads that take pieces as they
+// finish the last: a thread that the OS puts aside (another thread of the
+// process spinning on a CUDA event, say) holds up one piece, not 1/nt of
+// the job.
+void parallel_columns(int nt, size_t width, size_t cols, const std::function<void(size_t, size_t)>& body) {
+    const size_t per = std::max<size_t>(1, (size_t)(2u << 20) / std::max<size_t>(width, 1));
+    const size_t pieces = (cols + per - 1) / per;
+    std::atomic<size_t> next{0};
+    host_pool().run(std::min<int>(nt, (int)std::max<size_t>(pieces, 1)), [&](int) {
+        for (size_t q = next++; q < pieces; q = next++) body(q * per, std::min(cols, (q + 1) * per));
+    });
+}
+
 // Copies `cols` columns of `width` bytes between pitched layouts on `nt` threads.
 void parallel_copy(char* dst, size_t dpitch, const char* src, size_t spitch, size_t width, size_t cols) {
     const size_t bytes = width * cols;
     const int nt = bytes < (8u << 20) ? 1 : copy_threads();
-    auto work = [&](int t) {
-        const size_t c0 = cols * t / nt, c1 = cols * (t + 1) / nt;
+    parallel_columns(nt, width, cols, [&](size_t c0, size_t c1) {
         if (dpitch == width && spitch == width) {
             std::memcpy(dst + c0 * width, src + c0 * width, (c1 - c0) * width);
         } else {
             for (size_t c = c0; c < c1; ++c) std::memcpy(dst + c * dpitch, src + c * spitch, width);
         }
-    };
-    if (nt == 1) {
-        work(0);
-        return;
-    }
-    std::vector<std::thread> th;
-    th.reserve(nt - 1);
-    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
-    work(0);
-    for (auto& x : th) x.join();
+    });
 }
 
 enum class HostMem { Device, PinnedMapped, PinnedOther, Pageable };
@@ -160,15 +248,7 @@ void prefault(const void* base, size_t pitch, size_t width, size_t cols, bool wr
         (void)sink;
     };
     const int nt = width * cols < (8u << 20) ? 1 : copy_threads();
-    if (nt == 1) {
-        work(0, cols);
-        return;
-    }
-    std::vector<std::thread> th;
-    th.reserve(nt - 1);
-    for (int t = 1; t < nt; ++t) th.emplace_back(work, cols * t / nt, cols * (t + 1) / nt);
-    work(0, cols / nt);
-    for (auto& x : th) x.join();
+    parallel_columns(nt, width, cols, work);
 }
 
 // The copy as a device kernel (op N pack, 16-byte vectors where aligned)
@@ -198,6 +278,11 @@ bool direct_copy(void* dst, size_t dpitch, const void* src, size_t spitch, size_
 
 }  // namespace
 
+int staged_h2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+               cudaStream_t s);
+int staged_d2h(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+               cudaStream_t s);
+
 bool prepare_direct_host(void* p, size_t pitch, size_t width, size_t cols, bool write) {
     const HostMem hm = host_mem(p);
     if (hm != HostMem::Pageable && hm != HostMem::PinnedMapped) return false;
@@ -211,6 +296,29 @@ int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
     int st = COSMA_GPU_SUCCESS;
     if (direct_copy(dst, dpitch, src, spitch, width, cols, false, s, &st)) return st;
+    return staged_h2d(dst, dpitch, src, spitch, width, cols, s);
+}
+
+int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                cudaStream_t s) {
+    if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    int st = COSMA_GPU_SUCCESS;
+    if (direct_copy(dst, dpitch, src, spitch, width, cols, true, s, &st)) {
+        CGB_CHECK(st);
+        CGB_CUDA(cudaStreamSynchronize(s));
+        return COSMA_GPU_SUCCESS;
+    }
+    return staged_d2h(dst, dpitch, src, spitch, width, cols, s);
+}
+
+// Pageable host memory through the pinned staging buffers: host threads
+// copy column blocks into one buffer while the DMA engine moves the other.
+// The H2D form returns once every block is handed to the DMA engine, the
+// D2H form once the data is in host memory.  Page-locked memory, columns
+// wider than a staging buffer or staging buffers that cannot be had take
+// cudaMemcpy2DAsync.
+int staged_h2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+               cudaStream_t s) {
     const bool pg = pageable(src);
     std::lock_guard<std::mutex> lock(g_stage_mu);
     if (!pg || width > kStageBytes || !stager_ready()) {
@@ -230,15 +338,8 @@ int copy_h2d_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t
     return COSMA_GPU_SUCCESS;
 }
 
-int copy_d2h_2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
-                cudaStream_t s) {
-    if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
-    int st = COSMA_GPU_SUCCESS;
-    if (direct_copy(dst, dpitch, src, spitch, width, cols, true, s, &st)) {
-        CGB_CHECK(st);
-        CGB_CUDA(cudaStreamSynchronize(s));
-        return COSMA_GPU_SUCCESS;
-    }
+int staged_d2h(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+               cudaStream_t s) {
     const bool pg = pageable(dst);
     std::lock_guard<std::mutex> lock(g_stage_mu);
     if (!pg || width > kStageBytes || !stager_ready()) {
@@ -290,6 +391,15 @@ int copy_2d_overlapped(void* dst, size_t dpitch, const void* src, size_t spitch,
         return COSMA_GPU_SUCCESS;
     }
     return copy_2d_async(dst, dpitch, src, spitch, width, cols, kind, s);
+}
+
+int copy_2d_from_thread(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                        cudaMemcpyKind kind, cudaStream_t s) {
+    if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    if (kind == cudaMemcpyHostToDevice && pageable(src)) return staged_h2d(dst, dpitch, src, spitch, width, cols, s);
+    if (kind == cudaMemcpyDeviceToHost && pageable(dst)) return staged_d2h(dst, dpitch, src, spitch, width, cols, s);
+    CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, s));
+    return COSMA_GPU_SUCCESS;
 }
 
 bool host_direct_available() { return host_direct(); }

@@ -61,6 +61,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <chrono>
 #include <vector>
 
 namespace cgb {
@@ -1095,7 +1096,7 @@ private:
 // before any C is written, and when it differs, or the data holds Inf/NaN,
 // the call returns with *taken = false, C untouched and nothing in flight.
 struct PipeWorkspace {
-    DeviceBuffer a, b, resA, resB, expA, expB, part, R[2], C[2], stats, err;
+    DeviceBuffer a, b, resA, resB, expA, expB, part, R[8], C[8], stats, err;
     Stats* host_stats = nullptr;  // one record per panel
     unsigned* host_err = nullptr;
     std::vector<cudaEvent_t> ev;
@@ -1106,7 +1107,9 @@ struct PipeWorkspace {
 std::mutex g_pipe_mu;
 std::map<std::pair<int, cudaStream_t>, PipeWorkspace*> g_pipe;
 constexpr int kPipeMaxPanels = 16;
-constexpr int kPipeEvents = 48;
+constexpr int kPipeEvents = 64;
+constexpr int kPipeRing = 8;                        // blocks in flight: residue bytes and C slots
+constexpr size_t kPipeRingBytes = (size_t)8 << 30;  // at most this much HBM for the ring, 2 blocks at least
 
 PipeWorkspace* pipe_workspace(cudaStream_t s) {
     int dev = 0;
@@ -1159,18 +1162,22 @@ void release_pipe_workspace(cudaStream_t s) {
 }
 
 // Panel split of one dimension: `parts` pieces, each a multiple of 256 rows
-// (the CTA-pair tile) but the last.
+// (the CTA-pair tile) but the last, where the first (the lead panel) may be
+// shorter than the others: the first block can start once less data has
+// crossed the link.
 struct Panels {
     int count = 1;
-    int64_t size = 0;
-    int64_t first(int i) const { return (int64_t)i * size; }
-    int64_t rows(int i, int64_t total) const { return std::min(size, total - first(i)); }
+    int64_t lead = 0, size = 0;
+    int64_t first(int i) const { return i == 0 ? 0 : lead + (int64_t)(i - 1) * size; }
+    int64_t rows(int i, int64_t total) const { return std::min(i == 0 ? lead : size, total - first(i)); }
+    int64_t largest() const { return std::max(lead, size); }
 };
 
-Panels make_panels(int64_t total, int parts) {
+Panels make_panels(int64_t total, int parts, int64_t lead_max) {
     Panels p;
     p.size = ceil_div(ceil_div(total, parts), 256) * 256;
-    p.count = (int)ceil_div(total, p.size);
+    p.lead = std::min(p.size, lead_max);
+    p.count = 1 + (int)ceil_div(std::max<int64_t>(total - p.lead, 0), p.size);
     return p;
 }
 
@@ -1193,8 +1200,11 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     const int64_t m = g.m, n = g.n, k = g.k;
     if (g.scalar != Scalar::D || k > KMAX || k < 1 || m < 1 || n < 1) return COSMA_GPU_SUCCESS;
     const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
-    const Panels PA = make_panels(m, m >= 2048 ? 2 : 1);
-    const Panels PB = make_panels(n, n >= 4096 ? 4 : (n >= 2048 ? 2 : 1));
+    // op(A) in 2 row panels, the first cut to 2048 rows; op(B) in up to 4
+    // column panels.  At 16384^3 the first block waits for 0.75 GB instead of
+    // 1.5 GB.
+    const Panels PA = make_panels(m, m >= 2048 ? 2 : 1, 2048);
+    const Panels PB = make_panels(n, n >= 4096 ? 4 : (n >= 2048 ? 2 : 1), n);
     const int MA = PA.count, NB = PB.count, NP = MA + NB;
     if (MA * NB < 2 || NP > kPipeMaxPanels) return COSMA_GPU_SUCCESS;
     PipeWorkspace* w = pipe_workspace(cs);
@@ -1221,15 +1231,14 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         offB[j] = b_elems; b_elems += PB.rows(j, n) * k;
         eoffB[j] = eb; eb += ceil_div(PB.rows(j, n), BN) * BN;
     }
-    const int64_t ma_pad = ceil_div(PA.size, 2 * BM) * 2 * BM, nb_pad = ceil_div(PB.size, BN) * BN;
+    const int64_t ma_pad = ceil_div(PA.largest(), 2 * BM) * 2 * BM, nb_pad = ceil_div(PB.largest(), BN) * BN;
     // everything that could allocate is reserved before the first copy: a
     // growing buffer frees its old memory, which waits for the whole device
     CGB_CHECK(w->a.reserve((size_t)a_elems * 8, cs));
     CGB_CHECK(w->b.reserve((size_t)b_elems * 8, cs));
     CGB_CHECK(w->expA.reserve((size_t)ea * 4, cs));
     CGB_CHECK(w->expB.reserve((size_t)eb * 4, cs));
-    CGB_CHECK(w->part.reserve((size_t)64 * std::max(PA.size, PB.size) * 12, cs));
-    for (auto& c : w->C) CGB_CHECK(c.reserve((size_t)PA.size * PB.size * 8, cs));
+    CGB_CHECK(w->part.reserve((size_t)64 * std::max(PA.largest(), PB.largest()) * 12, cs));
     CGB_CHECK(w->stats.reserve((size_t)NP * sizeof(Stats), cs));
     CGB_CHECK(w->err.reserve(sizeof(unsigned), cs));
     Stats* sdev = (Stats*)w->stats.ptr;
@@ -1249,36 +1258,47 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     *h2d_bytes = 0;
     *d2h_bytes = 0;
 
-    // Host copies go through the copy engines (copy kernels would take SM room
-    // the persistent GEMMs wait for), issued by the copy worker.
+    // The first panel of each operand crosses before any kernel of the call
+    // runs, so a pageable one may take the device copy kernel (at the link's
+    // rate); every later copy runs beside the persistent GEMMs, whose CTAs a
+    // copy kernel would hold up, and goes through the copy engines, issued by
+    // the copy thread (pageable memory through the pinned staging buffers).
     CopyWorker& cw = *w->worker;
     auto copy_task = [](void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                         cudaMemcpyKind kind, cudaStream_t st, cudaEvent_t wait_ev, cudaEvent_t done_ev) {
         return [=]() -> int {
             if (wait_ev) CGB_CUDA(cudaStreamWaitEvent(st, wait_ev, 0));
-            CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, st));
+            CGB_CHECK(copy_2d_from_thread(dst, dpitch, src, spitch, width, cols, kind, st));
             CGB_CUDA(cudaEventRecord(done_ev, st));
             return COSMA_GPU_SUCCESS;
         };
     };
     uint64_t tk_copy[kPipeMaxPanels] = {};
+    auto copy_in = [&](int p, void* dst, size_t dpitch, const void* src, size_t spitch, size_t width,
+                       size_t cols) -> int {
+        if (p == 0 || p == MA) {
+            CGB_CHECK(copy_2d_overlapped(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, hs));
+            CGB_CUDA(cudaEventRecord(ev_copy[p], hs));
+            tk_copy[p] = 0;  // nothing to wait for on the copy thread
+        } else {
+            tk_copy[p] = cw.post(copy_task(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, hs,
+                                           nullptr, ev_copy[p]));
+        }
+        return COSMA_GPU_SUCCESS;
+    };
     // device copy of op(A) rows / op(B) columns of one panel, compact
     auto copy_panel = [&](int p) -> int {
         ev_copy[p] = next_event();
         if (p < MA) {
             const int64_t i0 = PA.first(p), mi = PA.rows(p, m);
-            if (!a_kc) tk_copy[p] = cw.post(copy_task(dA + offA[p], mi * 8, A + i0, g.lda * 8, mi * 8, k,
-                                                      cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
-            else tk_copy[p] = cw.post(copy_task(dA + offA[p], k * 8, A + i0 * g.lda, g.lda * 8, k * 8, mi,
-                                                cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
+            if (!a_kc) CGB_CHECK(copy_in(p, dA + offA[p], mi * 8, A + i0, g.lda * 8, mi * 8, k));
+            else CGB_CHECK(copy_in(p, dA + offA[p], k * 8, A + i0 * g.lda, g.lda * 8, k * 8, mi));
             *h2d_bytes += mi * k * 8;
         } else {
             const int j = p - MA;
             const int64_t j0 = PB.first(j), nj = PB.rows(j, n);
-            if (b_kc) tk_copy[p] = cw.post(copy_task(dB + offB[j], k * 8, B + j0 * g.ldb, g.ldb * 8, k * 8, nj,
-                                                     cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
-            else tk_copy[p] = cw.post(copy_task(dB + offB[j], nj * 8, B + j0, g.ldb * 8, nj * 8, k,
-                                                cudaMemcpyHostToDevice, hs, nullptr, ev_copy[p]));
+            if (b_kc) CGB_CHECK(copy_in(p, dB + offB[j], k * 8, B + j0 * g.ldb, g.ldb * 8, k * 8, nj));
+            else CGB_CHECK(copy_in(p, dB + offB[j], nj * 8, B + j0, g.ldb * 8, nj * 8, k));
             *h2d_bytes += nj * k * 8;
         }
         return COSMA_GPU_SUCCESS;
@@ -1334,7 +1354,20 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     for (int j = 0; j < NB; ++j) { roffB[j] = rb; rb += (int64_t)N * ceil_div(PB.rows(j, n), BN) * BN * k_pad; }
     CGB_CHECK(w->resA.reserve((size_t)ra * 2, cs));  // nothing in flight: the first panels are in
     CGB_CHECK(w->resB.reserve((size_t)rb * 2, cs));
-    for (auto& r : w->R) CGB_CHECK(r.reserve((size_t)N * ma_pad * nb_pad, cs));
+    // A ring of NR blocks in flight, each with the residue bytes of its
+    // modular GEMM and a C slot: NR blocks are queued before the host has
+    // checked every panel's statistics (the wait is for the last panel to
+    // cross), and after the check each block's reconstruction follows its
+    // GEMM directly, so that one reconstruction and one copy-out remain
+    // after the last GEMM.
+    const int NBLK = MA * NB;
+    const size_t r_bytes = (size_t)N * ma_pad * nb_pad, c_bytes = (size_t)PA.largest() * PB.largest() * 8;
+    int NR = std::min(NBLK, kPipeRing);
+    while (NR > 2 && (size_t)NR * (r_bytes + c_bytes) > kPipeRingBytes) --NR;
+    for (int r = 0; r < NR; ++r) {
+        CGB_CHECK(w->R[r].reserve(r_bytes, cs));
+        CGB_CHECK(w->C[r].reserve(c_bytes, cs));
+    }
 
     // 2. the other panels: B's first (block row 0 uses them), then A's
     std::vector<int> order;
@@ -1371,8 +1404,8 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         CGB_CUDA(cudaGetLastError());
         return COSMA_GPU_SUCCESS;
     };
-    // block b = i NB + j (row-major): its residue bytes go to R[b % 2], which
-    // the reconstruction of block b - 2 has read by then (same stream)
+    // block b = i NB + j (row-major): its residue bytes go to R[b % NR], which
+    // the reconstruction of block b - NR has read by then (same stream)
     auto gemm_block = [&](int b) -> int {
         const int i = b / NB, j = b % NB;
         CGB_CHECK(split_panel(i));
@@ -1380,27 +1413,36 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         const int64_t mi_pad = ceil_div(PA.rows(i, m), 2 * BM) * 2 * BM;
         const int64_t nj_pad = ceil_div(PB.rows(j, n), BN) * BN;
         GemmParams gp;
-        fill_gemm(gp, N, mi_pad, nj_pad, k_pad, w->R[b & 1].ptr, (unsigned*)w->err.ptr);
+        fill_gemm(gp, N, mi_pad, nj_pad, k_pad, w->R[b % NR].ptr, (unsigned*)w->err.ptr);
         return launch_gemm((uint16_t*)w->resA.ptr + roffA[i], (uint16_t*)w->resB.ptr + roffB[j], k_pad, gp, cs);
     };
 
-    // 3. the first two blocks start while the other panels are on the way
-    // (two, so that a slow link leaves the GPU work until the last panel is
-    // in); every other panel is scaled as it lands.  A panel's scale kernels
-    // are issued once its copy task has run (for pageable memory, once the
-    // copy itself is done), so block 0 is launched first.
-    const int NBLK = MA * NB;
+    // 3. the first NR blocks start while the other panels are on the way,
+    // so that the GPU has work until every panel is in and checked; every
+    // other panel is scaled as it lands.  A panel's scale kernels are issued
+    // once its copy task has run (for pageable memory, once the copy itself
+    // is done), so block 0 is launched first and each later block once its
+    // panels are in.
     CGB_CHECK(gemm_block(0));
-    CGB_CHECK(ensure_scaled(1 / NB));
-    CGB_CHECK(ensure_scaled(MA + (1 % NB)));
-    CGB_CHECK(gemm_block(1));
+    for (int b = 1; b < NR; ++b) {
+        CGB_CHECK(ensure_scaled(b / NB));
+        CGB_CHECK(ensure_scaled(MA + b % NB));
+        CGB_CHECK(gemm_block(b));
+    }
     for (int p : order) CGB_CHECK(ensure_scaled(p));
     cudaEvent_t ev_stats = next_event();
     CGB_CUDA(cudaMemcpyAsync(w->host_stats, sdev, (size_t)NP * sizeof(Stats), cudaMemcpyDeviceToHost, ss));
     CGB_CUDA(cudaEventRecord(ev_stats, ss));
     // every panel's statistics, then the check that the first panels chose
-    // the modulus count the whole data gives
-    CGB_CUDA(cudaEventSynchronize(ev_stats));
+    // the modulus count the whole data gives.  The wait sleeps between polls:
+    // a spinning thread would take a core from the host threads that copy
+    // pageable panels meanwhile.
+    for (;;) {
+        const cudaError_t q = cudaEventQuery(ev_stats);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) CGB_CUDA(q);
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
     std::vector<int> all(NP);
     for (int p = 0; p < NP; ++p) all[p] = p;
     const Stats sa = merge_stats(w->host_stats, all);
@@ -1417,20 +1459,36 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
 
     // 4. blocks in order; block b's C leaves on ds while block b+1 computes.
     // From here the call owns C: an error is the caller's, not a fall-back.
+    // A pageable C on a host whose page tables the device uses is read and
+    // written in place by the reconstruction kernel instead (its stores cross
+    // the link; no C slot, C-in or copy-out): the copies of pageable memory
+    // from the copy thread go through host threads and the staging buffers,
+    // whose rate does not keep up with both operands and C.
     *taken = true;
+    const bool c_direct =
+        !host_page_locked(C) && prepare_direct_host(C, (size_t)g.ldc * 8, (size_t)m * 8, (size_t)n, true);
     CombineParams cp0;
     fill_combine(cp0, N, pl.P);
-    cudaEvent_t ev_comb[2] = {next_event(), next_event()}, ev_out[2] = {next_event(), next_event()},
-                ev_cin[2] = {next_event(), next_event()};
-    bool out_used[2] = {false, false};
-    uint64_t tk_out[2] = {0, 0};  // the copy-out of each C slot
+    cudaEvent_t ev_comb[kPipeRing], ev_out[kPipeRing], ev_cin[kPipeRing];
+    for (int r = 0; r < NR; ++r) {
+        ev_comb[r] = next_event();
+        ev_out[r] = next_event();
+        ev_cin[r] = next_event();
+    }
+    bool out_used[kPipeRing] = {};
+    uint64_t tk_out[kPipeRing] = {};  // the copy-out of each C slot
     for (int b = 0; b < NBLK; ++b) {
+        // blocks 0 .. NR-1 are queued; block b >= NR takes the ring entry of
+        // block b - NR, whose reconstruction is ahead of it on the stream
+        if (b >= NR) CGB_CHECK(gemm_block(b));
         {
             const int i = b / NB, j = b % NB;
             const int64_t i0 = PA.first(i), mi = PA.rows(i, m), j0 = PB.first(j), nj = PB.rows(j, n);
-            const int slot = b & 1;
-            double* cdev = (double*)w->C[slot].ptr;
-            if (!beta_zero) {  // the old C block comes in once its slot has been drained
+            const int slot = b % NR;
+            double* cdev = c_direct ? C + i0 + j0 * g.ldc : (double*)w->C[slot].ptr;
+            if (c_direct) {
+                if (!beta_zero) *h2d_bytes += mi * nj * 8;
+            } else if (!beta_zero) {  // the old C block comes in once its slot has been drained
                 const uint64_t t = cw.post(copy_task(cdev, mi * 8, C + i0 + j0 * g.ldc, g.ldc * 8, mi * 8, nj,
                                                      cudaMemcpyHostToDevice, hs, out_used[slot] ? ev_out[slot] : nullptr,
                                                      ev_cin[slot]));
@@ -1444,12 +1502,12 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             CombineParams cp = cp0;
             cp.m = mi;
             cp.n = nj;
-            cp.ldc = mi;
+            cp.ldc = c_direct ? g.ldc : mi;
             cp.m_pad = ceil_div(mi, 2 * BM) * 2 * BM;
             cp.nb16 = ceil_div(nj, BN) * BN / 16;
             cp.n_split = INT64_MAX;
             cp.cs = 1;
-            cp.R = (const uint8_t*)w->R[b & 1].ptr;
+            cp.R = (const uint8_t*)w->R[slot].ptr;
             cp.expA = expA + eoffA[i];
             cp.expB = expB + eoffB[j];
             cp.C = cdev;
@@ -1458,13 +1516,14 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             cp.alpha_one = g.alpha[0] == 1.0;
             cp.beta_zero = beta_zero;
             CGB_CHECK(launch_combine(cp, N, nj, cs));
-            CGB_CUDA(cudaEventRecord(ev_comb[slot], cs));
-            tk_out[slot] = cw.post(copy_task(C + i0 + j0 * g.ldc, g.ldc * 8, cdev, mi * 8, mi * 8, nj,
-                                             cudaMemcpyDeviceToHost, ds, ev_comb[slot], ev_out[slot]));
             *d2h_bytes += mi * nj * 8;
-            out_used[slot] = true;
+            if (!c_direct) {
+                CGB_CUDA(cudaEventRecord(ev_comb[slot], cs));
+                tk_out[slot] = cw.post(copy_task(C + i0 + j0 * g.ldc, g.ldc * 8, cdev, mi * 8, mi * 8, nj,
+                                                 cudaMemcpyDeviceToHost, ds, ev_comb[slot], ev_out[slot]));
+                out_used[slot] = true;
+            }
         }
-        if (b + 2 < NBLK) CGB_CHECK(gemm_block(b + 2));  // after this block's reconstruction freed its R
     }
     CGB_CHECK(cw.drain());
     for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));

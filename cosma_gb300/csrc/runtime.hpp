@@ -173,6 +173,16 @@ int copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size
 // pageable memory as in copy_2d_async.
 int copy_2d_overlapped(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                        cudaMemcpyKind kind, cudaStream_t s);
+// A copy issued from a thread that may wait for it (the overlapped form's
+// copy thread): pageable host memory goes through the pinned staging buffers
+// (host threads and the copy engines: no SM is taken from running kernels,
+// and the driver's own pageable copies are avoided, whose speed swung
+// between 190 and 4 GB/s from one call to the next on the virtual machines
+// measured); page-locked memory through cudaMemcpy2DAsync.  For pageable
+// memory the H2D form returns once its data is handed to the copy engine,
+// the D2H form once it is in host memory; page-locked copies return at once.
+int copy_2d_from_thread(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                        cudaMemcpyKind kind, cudaStream_t s);
 // Whether the device copy kernel route is on (capable device, and
 // COSMA_GPU_HOST_DIRECT not OFF).
 bool host_direct_available();

@@ -283,8 +283,10 @@ def _tmm_call(ta, tb, m, n, k, A, B, C0, alpha, beta, ldc, pinned, overlap, monk
 
 
 @pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
-@pytest.mark.parametrize("ta,tb,beta", [("N", "N", 0.0), ("T", "N", 0.5), ("N", "T", -1.0), ("T", "T", 0.0)])
-def test_tiled_mm_overlapped_panels(native_lib, cuda, monkeypatch, ta, tb, beta, pinned):
+@pytest.mark.parametrize("ta,tb,beta,shape", [("N", "N", 0.0, (2100, 2300, 300)), ("T", "N", 0.5, (2100, 2300, 300)),
+                                              ("N", "T", -1.0, (2100, 2300, 300)), ("T", "T", 0.0, (2100, 2300, 300)),
+                                              ("T", "N", 0.5, (4500, 2300, 96)), ("N", "T", 0.0, (4500, 4200, 40))])
+def test_tiled_mm_overlapped_panels(native_lib, cuda, monkeypatch, ta, tb, beta, shape, pinned):
     """One-step Tiled-MM calls on host arrays (page-locked torch memory or
     pageable numpy arrays, whose copies a worker thread issues) large enough
     for the overlapped form (2 x 2 panels: op(A) rows and op(B) columns arrive
@@ -292,8 +294,11 @@ def test_tiled_mm_overlapped_panels(native_lib, cuda, monkeypatch, ta, tb, beta,
     overlap and of the device-pointer call; transfers count A and B (and C,
     when it is read) once.  Handles with two streams carry the C blocks on the
     copy stream.  The overlapped form times no phases (gemm_ms stays 0), which
-    tells it from the one-step form."""
-    m, n, k = 2100, 2300, 300
+    tells it from the one-step form.  With m >= 4096 the first op(A) panel is
+    a shorter lead panel (2048 rows, then 2304 and a ragged 148: 3 x 2
+    blocks; 3 x 4 with n = 4200), more blocks than the ring of residue
+    buffers holds."""
+    m, n, k = shape
     ldc = m + 3
     A = oracle.exp_spread(_op_shape(ta, m, k), 71, 4)
     B = oracle.exp_spread(_op_shape(tb, k, n), 72, 4)
