@@ -267,8 +267,7 @@ int cosma_gpu_zgemm_ozaki2_device(char transa, char transb, int64_t m, int64_t n
  * COSMA_GPU_OZAKI_NOALLOC_SCRATCH_BYTES; problems needing more are rejected
  * with COSMA_GPU_ERROR_INVALID_ARGUMENT and a message giving the size (about
  * m = n = k = 1024 with 13 slices fits).  The first call on each device looks
- * up the array's device address, so make it before any stream capture.  Each
- * call waits for its stream twice per pass over K (k beyond 65536 takes
+ * up the array's device address (cudaGetSymbolAddress).  Each call waits for its stream twice per pass over K (k beyond 65536 takes
  * several passes): once to read the exponent statistics that fix the slice
  * count, once to read the kernels' error word.  All calls share the one
  * array: calls that overlap on the GPU (other streams, other threads) race
