@@ -85,12 +85,12 @@ constexpr int64_t KMAX = 64 * 65535;  // K of one exact pass: the split grids' K
 
 // Residue matrices of a real (rows x k) operand: N BF16 matrices [t][rows_pad][k_pad]
 // (split_block), one block per 32 rows x 64 K elements.
-template <bool KCONTIG, int NL>
+template <bool KCONTIG, int NL, bool NARROW>
 __global__ void __launch_bounds__(256) split_kernel(const double* __restrict__ X, int64_t ld, int64_t rows,
                                                     int64_t k, const int* __restrict__ exps, int64_t k_pad,
                                                     int64_t rows_pad, uint16_t* __restrict__ out,
                                                     const __grid_constant__ SplitParams sp) {
-    split_block<KCONTIG, NL>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp, sp.P, blockIdx.x, blockIdx.y);
+    split_block<KCONTIG, NL, NARROW>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp, sp.P, blockIdx.x, blockIdx.y);
 }
 
 // Complex operands, laid out like the slice form's complex split: one real
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) split_cplx_kernel(const double2* __restri
             const int64_t l = l0 + e;
             double x = 0.0;
             if (r < rows && l < k) x = Xd[2 * (KCONTIG ? l + r * ld : r + l * ld) + part];
-            v[e] = scaled_integer(x, E, sp.P);
+            v[e] = scaled_integer<false>(x, E, sp.P);
             if (part && conj) v[e].sgn ^= 0x80000000u;  // the conjugated imaginary part
         }
 #pragma unroll 1
@@ -590,8 +590,15 @@ template <int NL>
 void launch_split_nl(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps,
                      int64_t k_pad, int64_t rows_pad, uint16_t* out, const SplitParams& sp, dim3 grid,
                      cudaStream_t st) {
-    if (kcontig) split_kernel<true, NL><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
-    else split_kernel<false, NL><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
+    if constexpr (NL <= 5) {
+        if (sp.P <= 63) {  // the scaled integers fit one 64-bit word
+            if (kcontig) split_kernel<true, NL, true><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
+            else split_kernel<false, NL, true><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
+            return;
+        }
+    }
+    if (kcontig) split_kernel<true, NL, false><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
+    else split_kernel<false, NL, false><<<grid, 256, 0, st>>>(X, ld, rows, k, exps, k_pad, rows_pad, out, sp);
 }
 
 void launch_split(bool kcontig, const double* X, int64_t ld, int64_t rows, int64_t k, const int* exps,

@@ -43,12 +43,15 @@ struct SplitParams {
 // The scaled integer X = round_half_away(|x| 2^(P - E)) of one operand
 // element as 13-bit limbs (X < 2^(P+1)), with its sign as an FP32 sign bit
 // (0x80000000 for negative x).  |x| = M 2^eu with the 53-bit significand M;
-// X = M 2^sh exactly when sh >= 0.
+// X = M 2^sh exactly when sh >= 0.  NARROW: P <= 63, so that X < 2^P fits
+// one 64-bit word (|x| < 2^E) and the limbs are fixed shifts of it; else X
+// is formed as a 128-bit integer.
 struct Scaled {
     uint32_t d[LIMB13];
     uint32_t sgn;
 };
 
+template <bool NARROW = false>
 __device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     Scaled v;
@@ -63,6 +66,12 @@ __device__ __forceinline__ Scaled scaled_integer(double x, int E, int P) {
         const int r = -sh;
         M = r > 63 ? 0ull : (M + (1ull << (r - 1))) >> r;
         sh = 0;
+    }
+    if constexpr (NARROW) {  // M << sh < 2^P <= 2^63 (sh <= 62 when M != 0)
+        const unsigned long long X = M << sh;
+#pragma unroll
+        for (int i = 0; i < LIMB13; ++i) v.d[i] = 13 * i < 64 ? (uint32_t)(X >> (13 * i)) & 0x1FFFu : 0u;
+        return v;
     }
     // X = M << sh as a 128-bit integer (hi:lo), then cut into 13-bit limbs
     unsigned long long lo, hi;
@@ -112,9 +121,14 @@ __device__ __forceinline__ uint32_t pair_signs(const Scaled& lo, const Scaled& h
 // threads, each 8 consecutive K elements of one row (one 16-byte store per
 // modulus).  A warp covers 4 rows x 64 K elements: its stores are four
 // 128-byte row segments per modulus, its loads (either layout) whole 32-byte
-// sectors.  kcontig: element (r, l) at X[l + r*ld], else at X[r + l*ld].  NL:
-// 13-bit limbs of the scaled integers (P < 13 NL).
-template <bool KCONTIG, int NL>
+// sectors; a K-contiguous row segment that is 16-byte aligned is read as four
+// 16-byte loads.  kcontig: element (r, l) at X[l + r*ld], else at
+// X[r + l*ld].  NL: 13-bit limbs of the scaled integers (P < 13 NL).
+// NARROW: P <= 63 (scaled_integer).  Measured at 16384^2 with 16 moduli
+// (P = 55): 3.11 ms for the M-contiguous layout and 2.47 ms for the
+// K-contiguous one, against 3.28 and 2.73 ms with the 128-bit form, scalar
+// loads and the modulus loop not unrolled.
+template <bool KCONTIG, int NL, bool NARROW = false>
 __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t k,
                                             const int* __restrict__ exps, int64_t k_pad, int64_t rows_pad,
                                             uint16_t* __restrict__ out, const SplitParams& sp, int P, int64_t bx,
@@ -125,20 +139,30 @@ __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_
     if (r >= rows_pad || l0 >= k_pad) return;
     const int E = r < rows ? exps[r] : 0;
     Scaled v[8];
+    const double* seg = X + (KCONTIG ? l0 + r * ld : r + l0 * ld);
+    if (KCONTIG && r < rows && l0 + 8 <= k && (reinterpret_cast<uintptr_t>(seg) & 15) == 0) {
+        const double2* s2 = reinterpret_cast<const double2*>(seg);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-        const int64_t l = l0 + e;
-        double x = 0.0;
-        if (r < rows && l < k) x = KCONTIG ? X[l + r * ld] : X[r + l * ld];
-        v[e] = scaled_integer(x, E, P);
+        for (int e = 0; e < 4; ++e) {
+            const double2 q = s2[e];
+            v[2 * e] = scaled_integer<NARROW>(q.x, E, P);
+            v[2 * e + 1] = scaled_integer<NARROW>(q.y, E, P);
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int64_t l = l0 + e;
+            double x = 0.0;
+            if (r < rows && l < k) x = KCONTIG ? X[l + r * ld] : X[r + l * ld];
+            v[e] = scaled_integer<NARROW>(x, E, P);
+        }
     }
     uint16_t* o = out + r * k_pad + l0;
     const int64_t slab = rows_pad * k_pad;
     uint32_t sg[4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) sg[e / 2] = pair_signs(v[e], v[e + 1]);
-#pragma unroll 1
-    for (int m = 0; m < sp.nmod; ++m) {
+    auto modulus = [&](int m) {
         const uint32_t p = sp.p[m], mg = sp.magic[m], h = sp.h[m];
         const float bias = sp.bias[m];
         uint32_t w[4];
@@ -147,6 +171,13 @@ __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_
             w[e / 2] = pack_bf16(residue_bits<NL>(v[e], p, mg, h, bias, sp.c13[m]),
                                  residue_bits<NL>(v[e + 1], p, mg, h, bias, sp.c13[m])) ^ sg[e / 2];
         *reinterpret_cast<uint4*>(o + m * slab) = make_uint4(w[0], w[1], w[2], w[3]);
+    };
+    if constexpr (KCONTIG) {
+#pragma unroll 1
+        for (int m = 0; m < sp.nmod; ++m) modulus(m);
+    } else {  // two moduli per trip: 5 % faster here, 6 % slower for the K-contiguous layout
+#pragma unroll 2
+        for (int m = 0; m < sp.nmod; ++m) modulus(m);
     }
 }
 
