@@ -396,6 +396,7 @@ int copy_2d_overlapped(void* dst, size_t dpitch, const void* src, size_t spitch,
 int copy_2d_from_thread(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
                         cudaMemcpyKind kind, cudaStream_t s) {
     if (width == 0 || cols == 0) return COSMA_GPU_SUCCESS;
+    if (inject_fault(kFaultHostCopy)) return set_error(COSMA_GPU_ERROR_CUDA, "host copy refused (injected fault)");
     if (kind == cudaMemcpyHostToDevice && pageable(src)) return staged_h2d(dst, dpitch, src, spitch, width, cols, s);
     if (kind == cudaMemcpyDeviceToHost && pageable(dst)) return staged_d2h(dst, dpitch, src, spitch, width, cols, s);
     CGB_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, cols, kind, s));

@@ -125,7 +125,7 @@ int cosma_gpu_last_error(void) { return cgb::t_last_code; }
 int cosma_gpu_test_fail_next(int site, int count) {
     cgb::clear_error();
     if (site <= 0 || site >= cgb::kFaultSites || count < 0)
-        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "test_fail_next: site 1..3 and count >= 0");
+        return cgb::set_error(COSMA_GPU_ERROR_INVALID_ARGUMENT, "test_fail_next: site 1..4 and count >= 0");
     cgb::g_faults[site].store(count);
     return COSMA_GPU_SUCCESS;
 }

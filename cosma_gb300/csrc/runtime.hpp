@@ -62,7 +62,13 @@ class PerDevice {
 // Host-side fault injection for tests (cosma_gpu_test_fail_next): each call
 // at an armed site consumes one pending fault and reports it, so the caller
 // takes its error path as if the CUDA call had failed.  No GPU is involved.
-enum FaultSite { kFaultDeviceAlloc = 1, kFaultHostRegister = 2, kFaultPinnedAlloc = 3, kFaultSites = 4 };
+enum FaultSite {
+    kFaultDeviceAlloc = 1,
+    kFaultHostRegister = 2,
+    kFaultPinnedAlloc = 3,
+    kFaultHostCopy = 4,  // a copy issued by the overlapped form's copy thread
+    kFaultSites = 5
+};
 bool inject_fault(int site);
 // cudaMallocHost behind the kFaultPinnedAlloc site.
 cudaError_t pinned_alloc(void** p, size_t bytes);

@@ -285,11 +285,15 @@ int cosma_gpu_dgemm_ozaki_noalloc(char transa, char transb, int64_t m, int64_t n
  * 2 page-locking of caller memory (cudaHostRegister: the streamer falls back
  * to its unregistered copy route, same result), 3 pinned staging allocations
  * (cudaMallocHost: an Ozaki / 3xBF16 call returns OUT_OF_MEMORY, the host
- * copies fall back to the driver's pageable copies).  count 0 disarms the
- * site.  Handles and contexts stay usable after an injected failure. */
+ * copies fall back to the driver's pageable copies), 4 a host copy issued by
+ * the overlapped one-step form's copy thread (the call returns
+ * COSMA_GPU_ERROR_CUDA with the copy's message; a refused operand-panel copy
+ * comes before any write to C).  count 0 disarms the site.  Handles and
+ * contexts stay usable after an injected failure. */
 #define COSMA_GPU_FAULT_DEVICE_ALLOC 1
 #define COSMA_GPU_FAULT_HOST_REGISTER 2
 #define COSMA_GPU_FAULT_PINNED_ALLOC 3
+#define COSMA_GPU_FAULT_HOST_COPY 4
 int cosma_gpu_test_fail_next(int site, int count);
 /* Faults still armed at `site` (-1 for an unknown site). */
 int cosma_gpu_test_faults_pending(int site);

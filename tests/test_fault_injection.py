@@ -5,19 +5,19 @@ these hooks let the tests drive those paths without faulting a GPU.  The GPU
 part (the error paths themselves) is tests/test_gpu_fault_injection.py."""
 import pytest
 
-DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC = 1, 2, 3
+DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC, HOST_COPY = 1, 2, 3, 4
 
 
 def test_hook_arms_and_disarms_each_site(native_lib):
     lib = native_lib
-    for site in (DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC):
+    for site in (DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC, HOST_COPY):
         assert lib.cosma_gpu_test_fail_next(site, 3) == 0
         assert lib.cosma_gpu_test_faults_pending(site) == 3
         assert lib.cosma_gpu_test_fail_next(site, 0) == 0
         assert lib.cosma_gpu_test_faults_pending(site) == 0
 
 
-@pytest.mark.parametrize("site,count", [(0, 1), (4, 1), (-1, 1), (1, -1)])
+@pytest.mark.parametrize("site,count", [(0, 1), (5, 1), (-1, 1), (1, -1)])
 def test_hook_rejects_bad_arguments(native_lib, site, count):
     lib = native_lib
     assert lib.cosma_gpu_test_fail_next(site, count) == 1  # COSMA_GPU_ERROR_INVALID_ARGUMENT

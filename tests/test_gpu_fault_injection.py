@@ -15,14 +15,14 @@ from gpu_util import from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
 
-DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC = 1, 2, 3
-OUT_OF_MEMORY = 3
+DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC, HOST_COPY = 1, 2, 3, 4
+OUT_OF_MEMORY, CUDA_ERROR = 3, 2
 
 
 @pytest.fixture(autouse=True)
 def disarm(native_lib):
     yield
-    for site in (DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC):
+    for site in (DEVICE_ALLOC, HOST_REGISTER, PINNED_ALLOC, HOST_COPY):
         native_lib.cosma_gpu_test_fail_next(site, 0)
 
 
@@ -163,4 +163,52 @@ def test_overlapped_form_allocation_failure_falls_back(native_lib, cuda, monkeyp
     again, info = run(h)  # the next call takes the overlapped form
     assert info["gemm_ms"] == 0.0
     np.testing.assert_array_equal(again, want)
+    h.close()
+
+
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+def test_overlapped_form_copy_failure_reported(native_lib, cuda, monkeypatch, pinned):
+    """A host copy refused inside the overlapped form's copy thread (the first
+    operand panel after the lead panels) fails the call with the copy's
+    status and message, reported on the calling thread; C is untouched, and
+    the next call on the same handle gives the bits of the form without
+    overlap."""
+    import torch
+
+    import cosma_gb300 as cg
+    from cosma_gb300 import CosmaGpuError
+    m, n, k = 2100, 2300, 300
+    A, B = oracle.uniform((m, k), 93), oracle.uniform((k, n), 94)
+    C0 = oracle.uniform((m, n), 95)
+
+    def host(X):
+        if not pinned:
+            return np.asfortranarray(X.copy())
+        return torch.from_numpy(np.ascontiguousarray(X.T).reshape(-1)).pin_memory()
+
+    def values(hC):
+        return hC.copy() if not pinned else hC.numpy().reshape(n, m).T.copy()
+
+    hA, hB = host(A), host(B)
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "OFF")
+    h = cg.make_context("d", 2)
+    h.set_method("ozaki2", 0)
+    hC = host(C0)
+    cg.gemm(h, "N", "N", m, n, k, 1.0, hA, m, hB, k, 0.5, hC, m)
+    want = values(hC)
+    h.close()
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "ON")
+    h = cg.make_context("d", 2)
+    h.set_method("ozaki2", 0)
+    hC = host(C0)
+    native_lib.cosma_gpu_test_fail_next(HOST_COPY, 1)
+    with pytest.raises(CosmaGpuError) as err:
+        cg.gemm(h, "N", "N", m, n, k, 1.0, hA, m, hB, k, 0.5, hC, m)
+    assert native_lib.cosma_gpu_test_faults_pending(HOST_COPY) == 0
+    assert err.value.code == CUDA_ERROR
+    assert "overlapped host copy" in str(err.value) and "injected" in str(err.value)
+    np.testing.assert_array_equal(values(hC), C0)  # nothing was written
+    cg.gemm(h, "N", "N", m, n, k, 1.0, hA, m, hB, k, 0.5, hC, m)
+    assert h.ozaki_info()["gemm_ms"] == 0.0  # the overlapped form ran
+    np.testing.assert_array_equal(values(hC), want)
     h.close()
