@@ -193,6 +193,19 @@ __global__ void gcheck_kernel(const Prob* __restrict__ P, const Stats* __restric
 }
 
 // ------------------------------------------------------------------ split
+template <int NL, bool NARROW>
+__device__ __forceinline__ void gsplit_item(const Prob& p, const Item& it, const SplitParams& sp) {
+    if (it.y == 0) {
+        if (p.akc) split_block<true, NL, NARROW>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w);
+        else split_block<false, NL, NARROW>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w);
+    } else {
+        if (p.bkc) split_block<true, NL, NARROW>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w);
+        else split_block<false, NL, NARROW>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w);
+    }
+}
+
+// One block of one problem's operand per CTA; a problem whose P is at most
+// 63 takes the 64-bit scaled integers (the branch is uniform over the CTA).
 template <int NL>
 __global__ void __launch_bounds__(256) gsplit_kernel(const Prob* __restrict__ P, const Item* __restrict__ items,
                                                      const int* __restrict__ ok,
@@ -200,13 +213,13 @@ __global__ void __launch_bounds__(256) gsplit_kernel(const Prob* __restrict__ P,
     const Item it = items[blockIdx.x];
     if (!ok[it.x]) return;
     const Prob& p = P[it.x];
-    if (it.y == 0) {
-        if (p.akc) split_block<true, NL>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w);
-        else split_block<false, NL>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w);
-    } else {
-        if (p.bkc) split_block<true, NL>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w);
-        else split_block<false, NL>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w);
+    if constexpr (NL <= 5) {
+        if (p.P <= 63) {
+            gsplit_item<NL, true>(p, it, sp);
+            return;
+        }
     }
+    gsplit_item<NL, false>(p, it, sp);
 }
 
 // ------------------------------------------------------------------- GEMM
