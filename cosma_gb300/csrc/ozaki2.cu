@@ -1560,6 +1560,13 @@ int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaS
         for (cudaStream_t s : {cs, hs, ds, w->ss})
             if (s) cudaStreamSynchronize(s);
         cudaGetLastError();
+        if (st == COSMA_GPU_ERROR_OUT_OF_MEMORY && !*taken) {
+            // the caller runs the regular path next, with its own workspace:
+            // this form's buffers go back first
+            for (DeviceBuffer* b : {&w->a, &w->b, &w->resA, &w->resB, &w->expA, &w->expB, &w->part}) b->release();
+            for (auto& r : w->R) r.release();
+            for (auto& c : w->C) c.release();
+        }
     }
     return st;
 }
