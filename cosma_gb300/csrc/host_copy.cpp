@@ -107,15 +107,19 @@ class HostPool {
         try {
             while ((int)th_.size() < want) {
                 const int id = (int)th_.size() + 1;
-                th_.emplace_back([this, id] { loop(id); });
+                unsigned long long now;
+                {
+                    std::lock_guard<std::mutex> lock(mu_);
+                    now = gen_;  // a new thread waits for the next job, not the last one
+                }
+                th_.emplace_back([this, id, now] { loop(id, now); });
             }
         } catch (...) {
-            return false;  // joined threads stay; this job runs alone
+            return false;  // the threads started so far stay; this job runs alone
         }
         return true;
     }
-    void loop(int id) {
-        unsigned long long seen = 0;
+    void loop(int id, unsigned long long seen) {
         for (;;) {
             const std::function<void(int)>* f;
             {
