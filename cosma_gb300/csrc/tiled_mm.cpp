@@ -234,8 +234,8 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     // One step on host operands with the Chinese-remainder method: the
     // overlapped form (op(A) / op(B) panels copied by the copy engines while
     // earlier blocks compute, C blocks copied out while later ones do) where
-    // it applies; 16384^3 from page-locked arrays took 99.5 to 101 ms per call
-    // in it against 116 ms in the one-step form.  Its copies are issued by a
+    // it applies; 16384^3 from page-locked arrays took 97 to 99 ms per call in
+    // it against 116 ms in the one-step form.  Its copies are issued by a
     // worker thread, so pageable arrays (whose copies return only once done)
     // overlap too.
     const bool overlap = env_bool("COSMA_GPU_OZAKI2_OVERLAP", true);
