@@ -60,9 +60,11 @@ constexpr int G_ACC = 4;  // TMEM accumulators of GBN columns
 static_assert(G_ACC * GBN <= 512, "TMEM columns");
 constexpr int G_SMEM = G_STAGES * G_STAGE + 1024 + 256;
 static_assert(G_SMEM <= 232448, "grouped GEMM shared memory");
-constexpr int EPI_WARPS = 8;  // two per TMEM lane quadrant, 64 columns each
+constexpr int EPI_WARPS = 16;                 // four per TMEM lane quadrant
+constexpr int EPI_GROUPS = EPI_WARPS / 4;     // column groups of a quadrant
 constexpr int G_THREADS = 64 + 32 * EPI_WARPS;
-constexpr int G_COLS = GBN / 2;
+constexpr int G_COLS = GBN / EPI_GROUPS;      // columns per epilogue thread
+static_assert(G_COLS % 32 == 0, "epilogue TMEM loads of 32 columns");
 
 // Device record of one problem (real data: op C is op T).
 struct Prob {
@@ -236,7 +238,7 @@ __device__ __forceinline__ void reduce_sums64(int (&s)[G_COLS], uint32_t p, uint
 // one residue byte per output.  Tiles of problems that failed the check are
 // skipped by all three roles alike.
 //   warp 0      TMA producer         warp 1   TMEM owner + MMA issuer
-//   warps 2..9  epilogue (TMEM -> registers -> residue bytes)
+//   warps 2..17 epilogue (TMEM -> registers -> residue bytes), four per TMEM lane quadrant
 __global__ void __launch_bounds__(G_THREADS, 1)
     oz2_grouped_gemm_kernel(const Prob* __restrict__ P, const CUtensorMap* __restrict__ maps,
                             const int4* __restrict__ units, int nunits, const int* __restrict__ okf, unsigned* err,
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         }
     } else {  // ------------------------------------------------ epilogue
         const int quad = warp & 3;          // TMEM lanes this warp may access
-        const int half = (warp - 2) >> 2;   // columns [half*64, half*64 + 64) of the tile
+        const int grp = (warp - 2) >> 2;    // columns [grp * G_COLS, (grp + 1) * G_COLS) of the tile
         const int row = quad * 32 + lane;
         uint32_t acc_it = 0;
         bool ok = true;
@@ -375,9 +377,9 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                         break;
                     }
                     tc::tc_fence_after();
-                    const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * GBN + half * G_COLS;
+                    const uint32_t base = tmem + ((uint32_t)(quad * 32) << 16) + buf * GBN + grp * G_COLS;
 #pragma unroll
-                    for (int q = 0; q < 2; ++q) {
+                    for (int q = 0; q < G_COLS / 32; ++q) {
                         uint32_t v[32];
                         tc::tmem_ld_32x32b_x32(base + q * 32, v);
                         tc::tmem_ld_wait();
@@ -391,9 +393,9 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                 }
                 if (!ok) break;
                 reduce_sums64(s, pm, mg, bias);
-                // the 64 residues of this thread's row: four groups of 16 columns
+                // the G_COLS residues of this thread's row, in groups of 16 columns
 #pragma unroll
-                for (int g = 0; g < 4; ++g) {
+                for (int g = 0; g < G_COLS / 16; ++g) {
                     uint32_t w[4];
 #pragma unroll
                     for (int b = 0; b < 4; ++b) {
@@ -401,7 +403,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
                         w[b] = (uint32_t)s[j0] | ((uint32_t)s[j0 + 1] << 8) | ((uint32_t)s[j0 + 2] << 16) |
                                ((uint32_t)s[j0 + 3] << 24);
                     }
-                    const int64_t jb = (int64_t)tl.z * (GBN / 16) + half * 4 + g;
+                    const int64_t jb = (int64_t)tl.z * (GBN / 16) + grp * (G_COLS / 16) + g;
                     *reinterpret_cast<uint4*>(R + (((int64_t)t * nb16 + jb) * m_pad + i) * 16) =
                         make_uint4(w[0], w[1], w[2], w[3]);
                 }
