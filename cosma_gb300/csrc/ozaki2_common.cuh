@@ -124,7 +124,9 @@ __device__ __forceinline__ uint32_t pair_signs(const Scaled& lo, const Scaled& h
 // sectors; a K-contiguous row segment that is 16-byte aligned is read as four
 // 16-byte loads.  kcontig: element (r, l) at X[l + r*ld], else at
 // X[r + l*ld].  NL: 13-bit limbs of the scaled integers (P < 13 NL).
-// NARROW: P <= 63 (scaled_integer).  Measured at 16384^2 with 16 moduli
+// NARROW: P <= 63 (scaled_integer).  keep_k_pad: the K padding [k, k_pad)
+// already holds zero residues (an arena zeroed once and never written there),
+// so threads wholly inside it return at once.  Measured at 16384^2 with 16 moduli
 // (P = 55): 3.11 ms for the M-contiguous layout and 2.47 ms for the
 // K-contiguous one, against 3.28 and 2.73 ms with the 128-bit form, scalar
 // loads and the modulus loop not unrolled.
@@ -132,11 +134,11 @@ template <bool KCONTIG, int NL, bool NARROW = false>
 __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_t ld, int64_t rows, int64_t k,
                                             const int* __restrict__ exps, int64_t k_pad, int64_t rows_pad,
                                             uint16_t* __restrict__ out, const SplitParams& sp, int P, int64_t bx,
-                                            int64_t by) {
+                                            int64_t by, bool keep_k_pad = false) {
     const int t = threadIdx.x;
     const int64_t r = bx * 32 + t / 8;
     const int64_t l0 = by * 64 + (t % 8) * 8;
-    if (r >= rows_pad || l0 >= k_pad) return;
+    if (r >= rows_pad || l0 >= (keep_k_pad ? k : k_pad)) return;
     const int E = r < rows ? exps[r] : 0;
     Scaled v[8];
     const double* seg = X + (KCONTIG ? l0 + r * ld : r + l0 * ld);

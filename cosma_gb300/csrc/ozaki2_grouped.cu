@@ -198,11 +198,11 @@ __global__ void gcheck_kernel(const Prob* __restrict__ P, const Stats* __restric
 template <int NL, bool NARROW>
 __device__ __forceinline__ void gsplit_item(const Prob& p, const Item& it, const SplitParams& sp) {
     if (it.y == 0) {
-        if (p.akc) split_block<true, NL, NARROW>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w);
-        else split_block<false, NL, NARROW>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w);
+        if (p.akc) split_block<true, NL, NARROW>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w, true);
+        else split_block<false, NL, NARROW>(p.A, p.lda, p.m, p.k, p.expA, p.k_pad, p.m, p.resA, sp, p.P, it.z, it.w, true);
     } else {
-        if (p.bkc) split_block<true, NL, NARROW>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w);
-        else split_block<false, NL, NARROW>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w);
+        if (p.bkc) split_block<true, NL, NARROW>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w, true);
+        else split_block<false, NL, NARROW>(p.B, p.ldb, p.n, p.k, p.expB, p.k_pad, p.n, p.resB, sp, p.P, it.z, it.w, true);
     }
 }
 
@@ -805,7 +805,8 @@ int build(Plan* pl, int count, const cosma_gpu_gemm_problem* in, int tune, cudaS
         r_bytes += align256((size_t)nmod * p.m_pad * p.n_pad);
     }
     CGB_CHECK(pl->res.reserve(std::max<size_t>(res_bytes, 256), st));
-    CGB_CUDA(cudaMemsetAsync(pl->res.ptr, 0, std::max<size_t>(res_bytes, 256), st));  // rows the split never writes
+    // rows past m (n) and K padding past k: the split never writes them
+    CGB_CUDA(cudaMemsetAsync(pl->res.ptr, 0, std::max<size_t>(res_bytes, 256), st));
     CGB_CHECK(pl->R.reserve(std::max<size_t>(r_bytes, 256), st));
     std::vector<CUtensorMap> maps(2 * cnt);
     std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
