@@ -285,7 +285,8 @@ def _tmm_call(ta, tb, m, n, k, A, B, C0, alpha, beta, ldc, pinned, overlap, monk
 @pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
 @pytest.mark.parametrize("ta,tb,beta,shape", [("N", "N", 0.0, (2100, 2300, 300)), ("T", "N", 0.5, (2100, 2300, 300)),
                                               ("N", "T", -1.0, (2100, 2300, 300)), ("T", "T", 0.0, (2100, 2300, 300)),
-                                              ("T", "N", 0.5, (4500, 2300, 96)), ("N", "T", 0.0, (4500, 4200, 40))])
+                                              ("T", "N", 0.5, (4500, 2300, 96)), ("N", "T", 0.0, (4500, 4200, 40)),
+                                              ("N", "N", 0.5, (1000, 4500, 64)), ("T", "T", -1.0, (2100, 2300, 1))])
 def test_tiled_mm_overlapped_panels(native_lib, cuda, monkeypatch, ta, tb, beta, shape, pinned):
     """One-step Tiled-MM calls on host arrays (page-locked torch memory or
     pageable numpy arrays, whose copies a worker thread issues) large enough
@@ -297,7 +298,7 @@ def test_tiled_mm_overlapped_panels(native_lib, cuda, monkeypatch, ta, tb, beta,
     tells it from the one-step form.  With m >= 4096 the first op(A) panel is
     a shorter lead panel (2048 rows, then 2304 and a ragged 148: 3 x 2
     blocks; 3 x 4 with n = 4200), more blocks than the ring of residue
-    buffers holds."""
+    buffers holds; one op(A) panel against four op(B) panels; k = 1."""
     m, n, k = shape
     ldc = m + 3
     A = oracle.exp_spread(_op_shape(ta, m, k), 71, 4)
