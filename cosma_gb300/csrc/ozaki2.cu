@@ -1092,8 +1092,9 @@ private:
     std::thread th_;  // last: started once everything it uses exists
 };
 
-// One-step DGEMM on host A, B and C (C = alpha op(A) op(B) + beta C), with the
-// host link's copies overlapped with the work: op(A) arrives in MA row panels
+// One-step DGEMM, or ZGEMM with real alpha and beta, on host A, B and C
+// (C = alpha op(A) op(B) + beta C), with the host link's copies overlapped
+// with the work: op(A) arrives in MA row panels
 // and op(B) in NB column panels on the copy stream, each panel's exponents
 // and statistics are taken as it lands, block (i, j)'s residue split and
 // modular GEMM start as soon as its two panels are in, and each block's C
@@ -1201,11 +1202,20 @@ Stats merge_stats(const Stats* s, const std::vector<int>& idx) {
     return r;
 }
 
-int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+int gemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
                               cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
     *taken = false;
     const int64_t m = g.m, n = g.n, k = g.k;
-    if (g.scalar != Scalar::D || k > KMAX || k < 1 || m < 1 || n < 1) return COSMA_GPU_SUCCESS;
+    const bool cplx = g.scalar == Scalar::Z;
+    if ((g.scalar != Scalar::D && !cplx) || k > KMAX || k < 1 || m < 1 || n < 1) return COSMA_GPU_SUCCESS;
+    // complex alpha / beta need a product buffer and an unpack per block: the
+    // regular path
+    if (cplx && (g.alpha[1] != 0.0 || g.beta[1] != 0.0)) return COSMA_GPU_SUCCESS;
+    // Complex operands follow the device ZGEMM's layout: op(A) rows
+    // [Re | sa Im] of 2 kh, op(B) columns as two stacked rows (Re C, Im C) of
+    // each block's GEMM; es doubles per element.
+    const int es = cplx ? 2 : 1;
+    const int64_t eb8 = 8 * es;  // bytes per element
     const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
     // op(A) in 2 row panels, the first cut to 2048 rows; op(B) in up to 4
     // column panels.  At 16384^3 the first block waits for 0.75 GB instead of
@@ -1221,7 +1231,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     if (!w->ss) return set_error(COSMA_GPU_ERROR_CUDA, "ozaki2: pipeline stream");
     if (!w->worker) return COSMA_GPU_SUCCESS;  // no copy thread: the regular path
     cudaStream_t ss = w->ss;
-    const int64_t k_pad = ceil_div(k, BKE) * BKE;
+    const int64_t kh = ceil_div(k, BKE) * BKE, k_pad = es * kh;
     const double* A = (const double*)g.A;
     const double* B = (const double*)g.B;
     double* C = (double*)g.C;
@@ -1241,8 +1251,8 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     const int64_t ma_pad = ceil_div(PA.largest(), 2 * BM) * 2 * BM, nb_pad = ceil_div(PB.largest(), BN) * BN;
     // everything that could allocate is reserved before the first copy: a
     // growing buffer frees its old memory, which waits for the whole device
-    CGB_CHECK(w->a.reserve((size_t)a_elems * 8, cs));
-    CGB_CHECK(w->b.reserve((size_t)b_elems * 8, cs));
+    CGB_CHECK(w->a.reserve((size_t)a_elems * eb8, cs));
+    CGB_CHECK(w->b.reserve((size_t)b_elems * eb8, cs));
     CGB_CHECK(w->expA.reserve((size_t)ea * 4, cs));
     CGB_CHECK(w->expB.reserve((size_t)eb * 4, cs));
     CGB_CHECK(w->part.reserve((size_t)64 * std::max(PA.largest(), PB.largest()) * 12, cs));
@@ -1298,15 +1308,15 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         ev_copy[p] = next_event();
         if (p < MA) {
             const int64_t i0 = PA.first(p), mi = PA.rows(p, m);
-            if (!a_kc) CGB_CHECK(copy_in(p, dA + offA[p], mi * 8, A + i0, g.lda * 8, mi * 8, k));
-            else CGB_CHECK(copy_in(p, dA + offA[p], k * 8, A + i0 * g.lda, g.lda * 8, k * 8, mi));
-            *h2d_bytes += mi * k * 8;
+            if (!a_kc) CGB_CHECK(copy_in(p, dA + offA[p] * es, mi * eb8, A + i0 * es, g.lda * eb8, mi * eb8, k));
+            else CGB_CHECK(copy_in(p, dA + offA[p] * es, k * eb8, A + i0 * g.lda * es, g.lda * eb8, k * eb8, mi));
+            *h2d_bytes += mi * k * eb8;
         } else {
             const int j = p - MA;
             const int64_t j0 = PB.first(j), nj = PB.rows(j, n);
-            if (b_kc) CGB_CHECK(copy_in(p, dB + offB[j], k * 8, B + j0 * g.ldb, g.ldb * 8, k * 8, nj));
-            else CGB_CHECK(copy_in(p, dB + offB[j], nj * 8, B + j0, g.ldb * 8, nj * 8, k));
-            *h2d_bytes += nj * k * 8;
+            if (b_kc) CGB_CHECK(copy_in(p, dB + offB[j] * es, k * eb8, B + j0 * g.ldb * es, g.ldb * eb8, k * eb8, nj));
+            else CGB_CHECK(copy_in(p, dB + offB[j] * es, nj * eb8, B + j0 * es, g.ldb * eb8, nj * eb8, k));
+            *h2d_bytes += nj * k * eb8;
         }
         return COSMA_GPU_SUCCESS;
     };
@@ -1317,13 +1327,13 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         CGB_CUDA(cudaStreamWaitEvent(ss, ev_copy[p], 0));
         if (p < MA) {
             const int64_t mi = PA.rows(p, m);
-            CGB_CHECK(oz::scale_operand(a_kc, dA + offA[p], a_kc ? k : mi, mi, k, expA + eoffA[p], w->part, sdev + p,
-                                        0, ss, 1));
+            CGB_CHECK(oz::scale_operand(a_kc, dA + offA[p] * es, a_kc ? k : mi, mi, k, expA + eoffA[p], w->part,
+                                        sdev + p, 0, ss, es));
         } else {
             const int j = p - MA;
             const int64_t nj = PB.rows(j, n);
-            CGB_CHECK(oz::scale_operand(b_kc, dB + offB[j], b_kc ? k : nj, nj, k, expB + eoffB[j], w->part,
-                                        sdev + p, 1, ss, 1));
+            CGB_CHECK(oz::scale_operand(b_kc, dB + offB[j] * es, b_kc ? k : nj, nj, k, expB + eoffB[j], w->part,
+                                        sdev + p, 1, ss, es));
         }
         ev_scaled[p] = next_event();
         CGB_CUDA(cudaEventRecord(ev_scaled[p], ss));
@@ -1349,7 +1359,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     if (s0.nonfinite) return abandon();
     Plan pl;
     pl.spread = (double)s0.spread[0] + (double)s0.spread[1];
-    if (choose(nmod_req, pl.spread, k, &pl.nmod, &pl.P, std::max(s0.exact_bits[0], s0.exact_bits[1])) !=
+    if (choose(nmod_req, pl.spread, es * k, &pl.nmod, &pl.P, std::max(s0.exact_bits[0], s0.exact_bits[1])) !=
         COSMA_GPU_SUCCESS) {
         clear_error();
         return abandon();
@@ -1358,7 +1368,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     std::vector<int64_t> roffA(MA), roffB(NB);
     int64_t ra = 0, rb = 0;
     for (int i = 0; i < MA; ++i) { roffA[i] = ra; ra += (int64_t)N * ceil_div(PA.rows(i, m), 2 * BM) * 2 * BM * k_pad; }
-    for (int j = 0; j < NB; ++j) { roffB[j] = rb; rb += (int64_t)N * ceil_div(PB.rows(j, n), BN) * BN * k_pad; }
+    for (int j = 0; j < NB; ++j) { roffB[j] = rb; rb += (int64_t)N * es * ceil_div(PB.rows(j, n), BN) * BN * k_pad; }
     CGB_CHECK(w->resA.reserve((size_t)ra * 2, cs));  // nothing in flight: the first panels are in
     CGB_CHECK(w->resB.reserve((size_t)rb * 2, cs));
     // A ring of NR blocks in flight, each with the residue bytes of its
@@ -1368,7 +1378,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     // GEMM directly, so that one reconstruction and one copy-out remain
     // after the last GEMM.
     const int NBLK = MA * NB;
-    const size_t r_bytes = (size_t)N * ma_pad * nb_pad, c_bytes = (size_t)PA.largest() * PB.largest() * 8;
+    const size_t r_bytes = (size_t)N * ma_pad * es * nb_pad, c_bytes = (size_t)PA.largest() * PB.largest() * eb8;
     int NR = std::min(NBLK, kPipeRing);
     while (NR > 2 && (size_t)NR * (r_bytes + c_bytes) > kPipeRingBytes) --NR;
     for (int r = 0; r < NR; ++r) {
@@ -1398,15 +1408,23 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         CGB_CUDA(cudaStreamWaitEvent(cs, ev_scaled[p], 0));
         if (p < MA) {
             const int64_t mi = PA.rows(p, m), mi_pad = ceil_div(mi, 2 * BM) * 2 * BM;
-            const dim3 grid((unsigned)(mi_pad / 32), (unsigned)(k_pad / 64));
-            launch_split(a_kc, dA + offA[p], a_kc ? k : mi, mi, k, expA + eoffA[p], k_pad, mi_pad,
-                         (uint16_t*)w->resA.ptr + roffA[p], sp, grid, cs);
+            const dim3 grid((unsigned)(mi_pad / 32), (unsigned)(kh / 64));
+            uint16_t* out = (uint16_t*)w->resA.ptr + roffA[p];
+            if (cplx)
+                launch_split_cplx(a_kc, false, (const double2*)(dA + offA[p] * 2), a_kc ? k : mi, mi, k, expA + eoffA[p],
+                                  kh, mi_pad, mi_pad, g.opa == 2, out, sp, grid, cs);
+            else
+                launch_split(a_kc, dA + offA[p], a_kc ? k : mi, mi, k, expA + eoffA[p], k_pad, mi_pad, out, sp, grid, cs);
         } else {
             const int j = p - MA;
             const int64_t nj = PB.rows(j, n), nj_pad = ceil_div(nj, BN) * BN;
-            const dim3 grid((unsigned)(nj_pad / 32), (unsigned)(k_pad / 64));
-            launch_split(b_kc, dB + offB[j], b_kc ? k : nj, nj, k, expB + eoffB[j], k_pad, nj_pad,
-                         (uint16_t*)w->resB.ptr + roffB[j], sp, grid, cs);
+            const dim3 grid((unsigned)(nj_pad / 32), (unsigned)(kh / 64));
+            uint16_t* out = (uint16_t*)w->resB.ptr + roffB[j];
+            if (cplx)
+                launch_split_cplx(b_kc, true, (const double2*)(dB + offB[j] * 2), b_kc ? k : nj, nj, k, expB + eoffB[j],
+                                  kh, nj_pad, 2 * nj_pad, g.opb == 2, out, sp, grid, cs);
+            else
+                launch_split(b_kc, dB + offB[j], b_kc ? k : nj, nj, k, expB + eoffB[j], k_pad, nj_pad, out, sp, grid, cs);
         }
         CGB_CUDA(cudaGetLastError());
         return COSMA_GPU_SUCCESS;
@@ -1420,7 +1438,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
         const int64_t mi_pad = ceil_div(PA.rows(i, m), 2 * BM) * 2 * BM;
         const int64_t nj_pad = ceil_div(PB.rows(j, n), BN) * BN;
         GemmParams gp;
-        fill_gemm(gp, N, mi_pad, nj_pad, k_pad, w->R[b % NR].ptr, (unsigned*)w->err.ptr);
+        fill_gemm(gp, N, mi_pad, es * nj_pad, k_pad, w->R[b % NR].ptr, (unsigned*)w->err.ptr);
         return launch_gemm((uint16_t*)w->resA.ptr + roffA[i], (uint16_t*)w->resB.ptr + roffB[j], k_pad, gp, cs);
     };
 
@@ -1457,7 +1475,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     Plan full;
     full.spread = (double)sa.spread[0] + (double)sa.spread[1];
     const int exact_bits = std::max(sa.exact_bits[0], sa.exact_bits[1]);
-    if (choose(nmod_req, full.spread, k, &full.nmod, &full.P, exact_bits) != COSMA_GPU_SUCCESS) {
+    if (choose(nmod_req, full.spread, es * k, &full.nmod, &full.P, exact_bits) != COSMA_GPU_SUCCESS) {
         clear_error();
         return abandon();
     }
@@ -1473,7 +1491,7 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
     // whose rate does not keep up with both operands and C.
     *taken = true;
     const bool c_direct =
-        !host_page_locked(C) && prepare_direct_host(C, (size_t)g.ldc * 8, (size_t)m * 8, (size_t)n, true);
+        !host_page_locked(C) && prepare_direct_host(C, (size_t)(g.ldc * eb8), (size_t)(m * eb8), (size_t)n, true);
     CombineParams cp0;
     fill_combine(cp0, N, pl.P);
     cudaEvent_t ev_comb[kPipeRing], ev_out[kPipeRing], ev_cin[kPipeRing];
@@ -1492,14 +1510,15 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             const int i = b / NB, j = b % NB;
             const int64_t i0 = PA.first(i), mi = PA.rows(i, m), j0 = PB.first(j), nj = PB.rows(j, n);
             const int slot = b % NR;
-            double* cdev = c_direct ? C + i0 + j0 * g.ldc : (double*)w->C[slot].ptr;
+            double* const chost = C + (i0 + j0 * g.ldc) * es;
+            double* cdev = c_direct ? chost : (double*)w->C[slot].ptr;
             if (c_direct) {
-                if (!beta_zero) *h2d_bytes += mi * nj * 8;
+                if (!beta_zero) *h2d_bytes += mi * nj * eb8;
             } else if (!beta_zero) {  // the old C block comes in once its slot has been drained
-                const uint64_t t = cw.post(copy_task(cdev, mi * 8, C + i0 + j0 * g.ldc, g.ldc * 8, mi * 8, nj,
+                const uint64_t t = cw.post(copy_task(cdev, mi * eb8, chost, g.ldc * eb8, mi * eb8, nj,
                                                      cudaMemcpyHostToDevice, hs, out_used[slot] ? ev_out[slot] : nullptr,
                                                      ev_cin[slot]));
-                *h2d_bytes += mi * nj * 8;
+                *h2d_bytes += mi * nj * eb8;
                 CGB_CHECK(cw.wait(t));
                 CGB_CUDA(cudaStreamWaitEvent(cs, ev_cin[slot], 0));
             } else if (out_used[slot]) {
@@ -1510,10 +1529,11 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             cp.m = mi;
             cp.n = nj;
             cp.ldc = c_direct ? g.ldc : mi;
+            const int64_t nj_pad = ceil_div(nj, BN) * BN;
             cp.m_pad = ceil_div(mi, 2 * BM) * 2 * BM;
-            cp.nb16 = ceil_div(nj, BN) * BN / 16;
-            cp.n_split = INT64_MAX;
-            cp.cs = 1;
+            cp.nb16 = es * nj_pad / 16;
+            cp.n_split = cplx ? nj_pad : INT64_MAX;  // complex: GEMM columns nj_pad.. are Im C
+            cp.cs = es;
             cp.R = (const uint8_t*)w->R[slot].ptr;
             cp.expA = expA + eoffA[i];
             cp.expB = expB + eoffB[j];
@@ -1522,11 +1542,11 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
             cp.beta = g.beta[0];
             cp.alpha_one = g.alpha[0] == 1.0;
             cp.beta_zero = beta_zero;
-            CGB_CHECK(launch_combine(cp, N, nj, cs));
-            *d2h_bytes += mi * nj * 8;
+            CGB_CHECK(launch_combine(cp, N, cplx ? 2 * nj_pad : nj, cs));
+            *d2h_bytes += mi * nj * eb8;
             if (!c_direct) {
                 CGB_CUDA(cudaEventRecord(ev_comb[slot], cs));
-                tk_out[slot] = cw.post(copy_task(C + i0 + j0 * g.ldc, g.ldc * 8, cdev, mi * 8, mi * 8, nj,
+                tk_out[slot] = cw.post(copy_task(chost, g.ldc * eb8, cdev, mi * eb8, mi * eb8, nj,
                                                  cudaMemcpyDeviceToHost, ds, ev_comb[slot], ev_out[slot]));
                 out_used[slot] = true;
             }
@@ -1551,9 +1571,9 @@ int dgemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, 
 
 // The overlapped form with its error exit: whatever fails, nothing is left in
 // flight on its streams when it returns.
-int dgemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+int gemm_host_pipelined(const GemmDesc& g, int nmod_req, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
                          cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
-    const int st = dgemm_host_pipelined_body(g, nmod_req, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
+    const int st = gemm_host_pipelined_body(g, nmod_req, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
     if (st != COSMA_GPU_SUCCESS) {
         PipeWorkspace* w = pipe_workspace(cs);
         if (w->worker) w->worker->drain();
@@ -1618,12 +1638,12 @@ void ozaki2_release_stream(cudaStream_t s) {
     oz2::release_pipe_workspace(s);
 }
 
-int ozaki2_dgemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+int ozaki2_gemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
                       cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken) {
     *taken = false;
     if (((uintptr_t)g.A | (uintptr_t)g.B | (uintptr_t)g.C) % 8) return COSMA_GPU_SUCCESS;
     if (g.m > (int64_t)1 << 24 || g.n > (int64_t)1 << 24) return COSMA_GPU_SUCCESS;
-    return oz2::dgemm_host_pipelined(g, moduli, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
+    return oz2::gemm_host_pipelined(g, moduli, cs, hs, ds, info, h2d_bytes, d2h_bytes, taken);
 }
 
 int ozaki2_dgemm(const GemmDesc& g, int moduli, cudaStream_t stream, cosma_gpu_ozaki_info* info) {

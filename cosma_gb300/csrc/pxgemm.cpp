@@ -160,6 +160,9 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
     // When its first panels would choose another modulus count than the whole
     // data, or the data holds Inf/NaN, or a buffer is refused before C is
     // touched, the staged path below runs.
+    // (pzgemm keeps the staged form: its unpack multiplies by alpha + 0i as a
+    // complex number, whose zero imaginary products can change the sign of a
+    // zero result, which the reconstruction's real scaling would not.)
     if (sc == Scalar::D && px_method() == COSMA_GPU_METHOD_OZAKI2 && !c_dev && !is_dev(asub) && !is_dev(bsub) &&
         env_bool("COSMA_GPU_OZAKI2_OVERLAP", true)) {
         for (auto& cs : g_px_copy)
@@ -167,7 +170,7 @@ int pxgemm_impl(Scalar sc, const char* transa, const char* transb, const int* pm
         const GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, asub, llda, bsub, lldb, beta, csub, lldc);
         int64_t h2d = 0, d2h = 0;
         bool taken = false;
-        const int st = ozaki2_dgemm_host(g, 0, s, g_px_copy[0], g_px_copy[1], nullptr, &h2d, &d2h, &taken);
+        const int st = ozaki2_gemm_host(g, 0, s, g_px_copy[0], g_px_copy[1], nullptr, &h2d, &d2h, &taken);
         if (taken && st == COSMA_GPU_SUCCESS) {
             g_px_h2d = h2d;
             g_px_d2h = d2h;

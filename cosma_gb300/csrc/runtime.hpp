@@ -144,13 +144,14 @@ int ozaki2_zgemm(const GemmDesc& g, int moduli, cudaStream_t stream,
 // destroyed (ozaki.cu, ozaki2.cu).
 void ozaki_release_stream(cudaStream_t s);
 void ozaki2_release_stream(cudaStream_t s);
-// One-step DGEMM on host A, B, C with the host copies overlapped with the
-// Chinese-remainder work (ozaki2.cu): cs computes, hs carries host-to-device
-// copies, ds device-to-host copies.  *taken = false (C untouched, nothing in
-// flight) when the shape does not pipeline, or when the first panels'
-// modulus count differs from the whole data's or the data holds Inf/NaN:
-// the caller then runs the regular path.
-int ozaki2_dgemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
+// One-step DGEMM, or ZGEMM with real alpha and beta, on host A, B, C with the
+// host copies overlapped with the Chinese-remainder work (ozaki2.cu): cs
+// computes, hs carries host-to-device copies, ds device-to-host copies.
+// *taken = false (C untouched, nothing in flight) when the shape or the
+// scalars do not pipeline, or when the first panels' modulus count differs
+// from the whole data's or the data holds Inf/NaN: the caller then runs the
+// regular path.
+int ozaki2_gemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
                       cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken);
 
 // The method of the process-wide entry points (p?gemm, multiply_using_layout):

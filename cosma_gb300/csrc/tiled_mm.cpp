@@ -231,8 +231,8 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     const int64_t ntiles = ntm * ntn, nsteps = ntiles * ntk;
     const bool keep_on_device = !dC && !copy_c_back;
     const bool crt = h->method == COSMA_GPU_METHOD_OZAKI2 && (sc == Scalar::D || sc == Scalar::Z);
-    // One step on host operands with the Chinese-remainder method: the
-    // overlapped form (op(A) / op(B) panels copied by the copy engines while
+    // One step on host operands with the Chinese-remainder method (double, or
+    // complex with real alpha and beta): the overlapped form (op(A) / op(B) panels copied by the copy engines while
     // earlier blocks compute, C blocks copied out while later ones do) where
     // it applies; 16384^3 from page-locked arrays took 97 to 99 ms per call in
     // it against 116 ms in the one-step form.  Its copies are issued by a
@@ -241,14 +241,13 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     const bool overlap = env_bool("COSMA_GPU_OZAKI2_OVERLAP", true);
     // With two streams the C blocks leave on the copy stream, behind every
     // panel copy (those end long before the first block is reconstructed).
-    if (overlap && crt && sc == Scalar::D && !dA && !dB && !dC && !trivial && !keep_on_device && nsteps == 1 &&
-        h->streams.size() >= 2) {
+    if (overlap && crt && !dA && !dB && !dC && !trivial && !keep_on_device && nsteps == 1 && h->streams.size() >= 2) {
         const GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
         cosma_gpu_ozaki_info oi{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
         int64_t h2d = 0, d2h = 0;
         bool taken = false;
         const size_t S = h->streams.size();
-        const int st = ozaki2_dgemm_host(g, h->slices, h->streams[0], h->streams[1],
+        const int st = ozaki2_gemm_host(g, h->slices, h->streams[0], h->streams[1],
                                          h->streams[std::min<size_t>(2, S - 1)], &oi, &h2d, &d2h, &taken);
         // a refused allocation before C is touched: the one-step form below
         // needs less memory

@@ -341,3 +341,64 @@ def test_tiled_mm_overlapped_falls_back(native_lib, cuda, monkeypatch, case, pin
     for key in ("slices", "fraction_bits", "exact_product", "fallback_native"):
         assert info[key] == info_off[key]
     assert info["fallback_native"] == (1 if case == "nan_late" else 0)
+
+
+def _host_matrix_z(A, pinned):
+    """Column-major complex host copy of A: pageable numpy or page-locked torch memory."""
+    import torch
+    if not pinned:
+        return np.asfortranarray(A), None
+    t = torch.from_numpy(np.ascontiguousarray(A.T).reshape(-1)).pin_memory()
+    return t, t
+
+
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+@pytest.mark.parametrize("ta,tb,alpha,beta", [("N", "N", 0.75, 0.0), ("T", "C", 1.0, 0.5), ("C", "N", -1.5, -1.0),
+                                              ("N", "T", 1.0, 0.0)])
+def test_tiled_mm_overlapped_complex(native_lib, cuda, monkeypatch, ta, tb, alpha, beta, pinned):
+    """ZGEMM through the Tiled-MM entry on host arrays in the overlapped
+    one-step form (real alpha and beta; op(B) columns become the two stacked
+    rows of each block's GEMM): the bits of the same call without overlap and
+    of the device call; a complex alpha keeps the regular one-step form."""
+    from cosma_gb300 import gemm, make_context, zgemm_ozaki2_device
+    m, n, k = 2100, 2300, 70
+    shp = lambda op, r, c: (r, c) if op == "N" else (c, r)
+    A = oracle.uniform(shp(ta, m, k), 101) + 1j * oracle.uniform(shp(ta, m, k), 102)
+    B = oracle.uniform(shp(tb, k, n), 103) + 1j * oracle.uniform(shp(tb, k, n), 104)
+    ldc = m + 2
+    C0 = np.zeros((ldc, n), dtype=np.complex128)
+    C0[:m] = oracle.uniform((m, n), 105) + 1j * oracle.uniform((m, n), 106)
+    outs = {}
+    for mode in ("ON", "OFF"):
+        monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", mode)
+        hA, _ = _host_matrix_z(A, pinned)
+        hB, _ = _host_matrix_z(B, pinned)
+        hC, tC = _host_matrix_z(C0, pinned)
+        h = make_context("z", 3)
+        h.set_method("ozaki2", 0)
+        gemm(h, ta, tb, m, n, k, alpha, hA, A.shape[0], hB, B.shape[0], beta, hC, ldc)
+        info = h.ozaki_info()
+        moved = h.transfer_bytes()
+        h.close()
+        out = tC.numpy().reshape(n, ldc).T if tC is not None else hC
+        outs[mode] = (np.array(out), info, moved)
+    on, info_on, moved = outs["ON"]
+    off, info_off, _ = outs["OFF"]
+    assert info_on["gemm_ms"] == 0.0 and info_off["gemm_ms"] > 0.0
+    assert info_on["slices"] == info_off["slices"]
+    assert on.tobytes() == off.tobytes()
+    np.testing.assert_array_equal(on[m:], C0[m:])  # rows past m untouched
+    assert moved == (16 * (m * k + k * n + (m * n if beta != 0 else 0)), 16 * m * n)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C0, ldc)
+    zgemm_ozaki2_device(ta, tb, m, n, k, alpha, dA, A.shape[0], dB, B.shape[0], beta, dC, ldc)
+    assert on[:m].tobytes() == np.ascontiguousarray(from_dev(dC, m, n, ldc)).tobytes()
+    # a complex alpha: the regular one-step form
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "ON")
+    hA, _ = _host_matrix_z(A, pinned)
+    hB, _ = _host_matrix_z(B, pinned)
+    hC, _ = _host_matrix_z(C0, pinned)
+    h = make_context("z", 3)
+    h.set_method("ozaki2", 0)
+    gemm(h, ta, tb, m, n, k, 0.5 + 0.25j, hA, A.shape[0], hB, B.shape[0], beta, hC, ldc)
+    assert h.ozaki_info()["gemm_ms"] > 0.0
+    h.close()
