@@ -50,7 +50,7 @@ def reference_available() -> bool:
 
 def build_ref(force: bool = False) -> Path | None:
     """Compiles the reference's CPU files into oracle/_ref/libcosma_ref.so;
-    None when the reference's sources are not present (e.g. on a GPU machine)."""
+    None when the reference's sources are not present."""
     if not reference_available():
         return REF_OUT if REF_OUT.exists() else None
     deps = [REF_ROOT / f for f in REF_FILES] + [HERE / "ref_shim.cpp"] + list((HERE / "ref_stubs").rglob("*"))

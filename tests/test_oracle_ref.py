@@ -5,7 +5,7 @@ lie - src/cosma/local_multiply.cpp (the naive local_multiply_cpu loop and the
 CPU build's local_multiply -> cosma::gemm), src/cosma/blas.cpp and
 src/cosma/scalapack.cpp (numroc) - into oracle/_ref/libcosma_ref.so, with
 stand-in headers for MPI / BLACS / COSTA and a CBLAS over scipy's OpenBLAS.
-Where the reference's sources are absent (a GPU machine) these tests skip.
+Where the reference's sources are absent these tests skip.
 """
 import ctypes as C
 import glob
