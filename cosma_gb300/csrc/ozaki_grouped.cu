@@ -189,9 +189,10 @@ constexpr int G_SMEM = G_STAGES * G_STAGE + 1024 + 256;
 static_assert(G_SMEM <= 232448, "grouped GEMM shared memory");
 // Eight epilogue warps, two per TMEM lane quadrant, each draining 32 of the
 // tile's 64 columns.
-constexpr int G_EPI_WARPS = 8;
+constexpr int G_EPI_WARPS = 16;                   // four per TMEM lane quadrant
 constexpr int G_THREADS = 64 + 32 * G_EPI_WARPS;
-constexpr int G_COLS = GBN / 2;  // columns per epilogue thread
+constexpr int G_COLS = GBN / (G_EPI_WARPS / 4);  // columns per epilogue thread
+static_assert(G_COLS % 16 == 0, "epilogue TMEM loads of 16 columns");
 
 // Drains the accumulator groups of one tile (rows mb*128.., this thread's 32
 // columns of nb*64..) into 128-bit partial sums held in registers and, after
@@ -223,16 +224,18 @@ __device__ __forceinline__ bool gepilogue_tile(const Prob& p, const Schedule& sc
         tc::tc_fence_after();
         const int sh = sc.gshift[g];
         uint32_t v[16];
-        tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c0, v);
-        tc::tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 16; ++j) add_shifted(lo[j], hi[j], __float2int_rn(__uint_as_float(v[j])), sh);
-        tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c0 + 16, v);
-        tc::tmem_ld_wait();
-        tc::tc_fence_before();
-        release(buf);  // the values are in registers: the issuer may reuse the accumulator
+        for (int q = 0; q < G_COLS / 16; ++q) {
+            tc::tmem_ld_32x32b_x16(tmem + lanes + buf * GBN + c0 + 16 * q, v);
+            tc::tmem_ld_wait();
+            if (q == G_COLS / 16 - 1) {
+                tc::tc_fence_before();
+                release(buf);  // the values are in registers: the issuer may reuse the accumulator
+            }
 #pragma unroll
-        for (int j = 0; j < 16; ++j) add_shifted(lo[16 + j], hi[16 + j], __float2int_rn(__uint_as_float(v[j])), sh);
+            for (int j = 0; j < 16; ++j)
+                add_shifted(lo[16 * q + j], hi[16 * q + j], __float2int_rn(__uint_as_float(v[j])), sh);
+        }
     }
 #pragma unroll
     for (int j = 0; j < G_COLS; ++j) {
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         }
     } else {  // ------------------------------------------------ epilogue
         const int quad = warp & 3;         // TMEM lanes this warp may access
-        const int half = (warp - 2) / 4;  // which 32 of the 64 columns
+        const int half = (warp - 2) / 4;  // which G_COLS of the 64 columns
         const uint64_t pol_stream = tc::policy_evict_first();
         uint32_t acc_it = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
