@@ -571,6 +571,7 @@ void fill_crt(CrtConst& cp, int nmod) {
         const uint32_t y = inverse_mod(Mt.mod_small(kModuli[t]), kModuli[t]);
         Mt.mul_small(y);
         std::memcpy(cp.w[t], Mt.w, sizeof(Mt.w));
+        for (int q = 0; q < 2 * LIMBS; ++q) cp.w16[t][q] = (Mt.w[q / 2] >> (16 * (q % 2))) & 0xFFFFu;
     }
     std::memcpy(cp.M, M.w, sizeof(M.w));
     // M / 2^(32 (L-2)) from its top three limbs, as the kernel forms X's

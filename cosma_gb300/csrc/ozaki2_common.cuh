@@ -188,6 +188,7 @@ __device__ __forceinline__ void split_block(const double* __restrict__ X, int64_
 struct CrtConst {
     int nmod;
     uint32_t w[MAX_MODULI][LIMBS];  // CRT weights w_t = (M/p_t) * ((M/p_t)^-1 mod p_t)
+    uint32_t w16[MAX_MODULI][2 * LIMBS];  // the same in 16-bit pieces, lowest first
     uint32_t M[LIMBS];
     float inv_m2;                   // 2^(32 (L-2)) / M for the quotient estimate (L = limbs_for(nmod))
 };
@@ -336,16 +337,20 @@ __device__ __forceinline__ bool reduce_crt(const unsigned long long (&acc)[L], u
 }
 
 // X_c = sum_t r_{t,c} w_t (L 64-bit partial limbs) for the four residue bytes
-// c of the words rp[t * stride], t < nmod.  The words of eight moduli are
-// loaded before their products are summed, so that eight loads are in
-// flight per thread.
+// c of the words rp[t * stride], t < nmod.  The sums run over the weights'
+// 16-bit pieces in 32-bit registers (at most 28 * 255 * 65535 < 2^29 each),
+// one integer multiply-add per piece, instead of 64-bit products and sums;
+// the pieces are folded into 64-bit partial limbs at the end.  The words of
+// eight moduli are loaded before their products are summed, so that eight
+// loads are in flight per thread.
 template <int L>
 __device__ __forceinline__ void crt_accumulate(const uint32_t* __restrict__ rp, int64_t stride, int nmod,
                                                const CrtConst& crt, unsigned long long (&acc)[4][L]) {
+    uint32_t a[4][2 * L];
 #pragma unroll
     for (int c = 0; c < 4; ++c)
 #pragma unroll
-        for (int l = 0; l < L; ++l) acc[c][l] = 0;
+        for (int q = 0; q < 2 * L; ++q) a[c][q] = 0;
 #pragma unroll 1
     for (int t0 = 0; t0 < nmod; t0 += 8) {
         uint32_t rr[8];
@@ -359,10 +364,15 @@ __device__ __forceinline__ void crt_accumulate(const uint32_t* __restrict__ rp, 
             for (int c = 0; c < 4; ++c) {
                 const uint32_t r = (rr[u] >> (8 * c)) & 0xFFu;
 #pragma unroll
-                for (int l = 0; l < L; ++l) acc[c][l] += (unsigned long long)r * crt.w[t][l];
+                for (int q = 0; q < 2 * L; ++q) a[c][q] += r * crt.w16[t][q];
             }
         }
     }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int l = 0; l < L; ++l)
+            acc[c][l] = (unsigned long long)a[c][2 * l] + ((unsigned long long)a[c][2 * l + 1] << 16);
 }
 
 // ---------------------------------------------------------------- host side
