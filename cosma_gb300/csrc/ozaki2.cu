@@ -1218,9 +1218,10 @@ int gemm_host_pipelined_body(const GemmDesc& g, int nmod_req, cudaStream_t cs, c
     const int es = cplx ? 2 : 1;
     const int64_t eb8 = 8 * es;  // bytes per element
     const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
-    // op(A) in row panels: a lead panel of at most 2048 rows, then halves of
-    // the rest; op(B) in up to 4 column panels.  At 16384^3 the first block
-    // waits for 0.75 GB instead of 1.5 GB.
+    // op(A) in row panels: a lead panel of at most 2048 rows, then panels of
+    // half the rows (the last one shorter: 2048, 8192, 6144 at m = 16384);
+    // op(B) in up to 4 column panels.  At 16384^3 the first block waits for
+    // 0.75 GB instead of 1.5 GB.
     const Panels PA = make_panels(m, m >= 2048 ? 2 : 1, 2048);
     const Panels PB = make_panels(n, n >= 4096 ? 4 : (n >= 2048 ? 2 : 1), n);
     const int MA = PA.count, NB = PB.count, NP = MA + NB;
