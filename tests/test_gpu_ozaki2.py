@@ -402,3 +402,37 @@ def test_tiled_mm_overlapped_complex(native_lib, cuda, monkeypatch, ta, tb, alph
     gemm(h, ta, tb, m, n, k, 0.5 + 0.25j, hA, A.shape[0], hB, B.shape[0], beta, hC, ldc)
     assert h.ozaki_info()["gemm_ms"] > 0.0
     h.close()
+
+
+def test_tiled_mm_overlapped_concurrent_handles(native_lib, cuda, monkeypatch):
+    """Two host threads, each with its own handle, run the overlapped form at
+    the same time on pageable arrays (two copy threads sharing the staging
+    buffers and the host copy pool): each gets the bits of the same call made
+    alone."""
+    import threading
+    from cosma_gb300 import gemm, make_context
+    monkeypatch.setenv("COSMA_GPU_OZAKI2_OVERLAP", "ON")
+    m, n, k = 2100, 2300, 64
+    cases = [(oracle.exp_spread((m, k), 111 + 2 * s, 3), oracle.exp_spread((k, n), 112 + 2 * s, 3)) for s in range(2)]
+
+    def run(A, B, out, idx):
+        h = make_context("d", 3)
+        h.set_method("ozaki2", 0)
+        C = np.zeros((m, n), order="F")
+        for _ in range(3):
+            gemm(h, "N", "N", m, n, k, 1.0, np.asfortranarray(A), m, np.asfortranarray(B), k, 0.0, C, m)
+        out[idx] = (C.copy(), h.ozaki_info()["gemm_ms"])
+        h.close()
+
+    alone = [None, None]
+    for i, (A, B) in enumerate(cases):
+        run(A, B, alone, i)
+    together = [None, None]
+    threads = [threading.Thread(target=run, args=(A, B, together, i)) for i, (A, B) in enumerate(cases)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for i in range(2):
+        assert together[i] is not None and together[i][1] == 0.0  # the overlapped form ran
+        assert together[i][0].tobytes() == alone[i][0].tobytes()
