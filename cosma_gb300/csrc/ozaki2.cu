@@ -47,6 +47,7 @@
 #include "ozaki2_common.cuh"
 #include "tc_common.cuh"
 #include "tma_host.hpp"
+#include "pipeline.hpp"
 
 #include <cuda_bf16.h>
 
@@ -1014,89 +1015,10 @@ int zgemm(const GemmDesc& g, int nmod_req, cudaStream_t st, cosma_gpu_ozaki_info
 }
 
 // ------------------------------------------------------ host operands, overlapped
-// Host copies issued from a worker thread, in order.  A copy of pageable
-// host memory returns only once it is done (even cudaMemcpy2DAsync), so the
-// thread that feeds the GPU must not issue it; page-locked copies return at
-// once either way.  post() queues a task and returns its ticket; wait(t)
-// returns once task t has run (its copy issued, or for pageable memory done,
-// and its event recorded), with the first error of the tasks so far.
-class CopyWorker {
-public:
-    explicit CopyWorker(int device) : device_(device), th_([this] { loop(); }) {}
-    ~CopyWorker() {
-        {
-            std::lock_guard<std::mutex> lock(mu_);
-            stop_ = true;
-        }
-        cv_.notify_all();
-        th_.join();
-    }
-    uint64_t post(std::function<int()> task) {
-        std::lock_guard<std::mutex> lock(mu_);
-        q_.push_back(std::move(task));
-        cv_.notify_all();
-        return ++posted_;
-    }
-    // An error of the worker's thread is reported again on the caller's (the
-    // library's last-error record is per thread).
-    int wait(uint64_t ticket) {
-        std::unique_lock<std::mutex> lock(mu_);
-        cv_.wait(lock, [&] { return done_ >= ticket; });
-        if (err_ != COSMA_GPU_SUCCESS) set_error(err_, msg_);
-        return err_;
-    }
-    int drain() {
-        uint64_t t;
-        {
-            std::lock_guard<std::mutex> lock(mu_);
-            t = posted_;
-        }
-        const int e = wait(t);
-        std::lock_guard<std::mutex> lock(mu_);
-        err_ = COSMA_GPU_SUCCESS;  // reported once
-        msg_.clear();
-        return e;
-    }
-
-private:
-    void loop() {
-        cudaSetDevice(device_);
-        for (;;) {
-            std::function<int()> task;
-            {
-                std::unique_lock<std::mutex> lock(mu_);
-                cv_.wait(lock, [&] { return stop_ || !q_.empty(); });
-                if (q_.empty()) return;  // stopping
-                task = std::move(q_.front());
-                q_.pop_front();
-            }
-            const int e = task();
-            {
-                std::lock_guard<std::mutex> lock(mu_);
-                if (e != COSMA_GPU_SUCCESS && err_ == COSMA_GPU_SUCCESS) {
-                    err_ = e;
-                    msg_ = std::string("overlapped host copy: ") + cosma_gpu_last_error_string();
-                }
-                ++done_;
-            }
-            cv_.notify_all();
-        }
-    }
-    int device_;
-    std::mutex mu_;
-    std::condition_variable cv_;
-    std::deque<std::function<int()>> q_;
-    uint64_t posted_ = 0, done_ = 0;
-    int err_ = COSMA_GPU_SUCCESS;
-    std::string msg_;
-    bool stop_ = false;
-    std::thread th_;  // last: started once everything it uses exists
-};
-
 // One-step DGEMM, or ZGEMM with real alpha and beta, on host A, B and C
 // (C = alpha op(A) op(B) + beta C), with the host link's copies overlapped
-// with the work: op(A) arrives in MA row panels
-// and op(B) in NB column panels on the copy stream, each panel's exponents
+// with the work: op(A) arrives in MA row panels and op(B) in NB column
+// panels on the copy stream, each panel's exponents
 // and statistics are taken as it lands, block (i, j)'s residue split and
 // modular GEMM start as soon as its two panels are in, and each block's C
 // leaves on its own stream while the next block computes.  The modulus count
@@ -1168,26 +1090,6 @@ void release_pipe_workspace(cudaStream_t s) {
     }
     delete w;
     cudaGetLastError();
-}
-
-// Panel split of one dimension: `parts` pieces, each a multiple of 256 rows
-// (the CTA-pair tile) but the last, where the first (the lead panel) may be
-// shorter than the others: the first block can start once less data has
-// crossed the link.
-struct Panels {
-    int count = 1;
-    int64_t lead = 0, size = 0;
-    int64_t first(int i) const { return i == 0 ? 0 : lead + (int64_t)(i - 1) * size; }
-    int64_t rows(int i, int64_t total) const { return std::min(i == 0 ? lead : size, total - first(i)); }
-    int64_t largest() const { return std::max(lead, size); }
-};
-
-Panels make_panels(int64_t total, int parts, int64_t lead_max) {
-    Panels p;
-    p.size = ceil_div(ceil_div(total, parts), 256) * 256;
-    p.lead = std::min(p.size, lead_max);
-    p.count = 1 + (int)ceil_div(std::max<int64_t>(total - p.lead, 0), p.size);
-    return p;
 }
 
 // Combined statistics of a set of panel records (A panels in field 0, B in 1).
