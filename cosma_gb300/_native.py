@@ -70,6 +70,7 @@ SIGNATURES = {
     "cosma_gpu_tmm_device_buffer_c": (vp, [vp]),
     "cosma_gpu_tmm_last_ozaki_info": (i32, [vp, C.POINTER(OzakiInfo)]),
     "cosma_gpu_tmm_last_transfer_bytes": (i32, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "cosma_gpu_tmm_last_overlapped": (i32, [vp]),
     "cosma_gpu_tmm_tiles_for_memory": (i32, [ch, i32, i64, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                              C.POINTER(C.c_int)]),
     "cosma_gpu_tmm_set_memory_limit": (i32, [vp, i64]),

@@ -87,6 +87,10 @@ class MMHandle:
         N.check(self.lib.cosma_gpu_tmm_tiles(self._h, *(C.byref(x) for x in t)))
         return tuple(x.value for x in t)
 
+    def last_overlapped(self) -> bool:
+        """Whether the last gemm call ran in an overlapped one-step form."""
+        return bool(self.lib.cosma_gpu_tmm_last_overlapped(self._h))
+
     def transfer_bytes(self):
         """(host->device, device->host) bytes moved by the last gemm call."""
         h2d, d2h = C.c_int64(), C.c_int64()

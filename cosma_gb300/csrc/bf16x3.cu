@@ -24,14 +24,17 @@
 #include "runtime.hpp"
 #include "tc_common.cuh"
 #include "tma_host.hpp"
+#include "pipeline.hpp"
 
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace cgb {
 namespace b3 {
@@ -280,6 +283,58 @@ Workspace* workspace(cudaStream_t s) {
 
 int num_sms() { return device_sm_count(); }
 
+// The GEMM kernel's shared-memory attribute, set once per device.
+int gemm_attr() {
+    static PerDevice<bool> attr;
+    bool done = false;
+    return attr.get(
+        [](bool& v) {
+            CGB_CUDA(cudaFuncSetAttribute(bf16x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          SMEM_BYTES));
+            v = true;
+            return COSMA_GPU_SUCCESS;
+        },
+        &done);
+}
+
+// The GEMM over slice stacks sa (3 x a_rows_pad rows) and sb (3 x b_rows_pad
+// rows) of K depth k_pad, into C (m x n, ldc).
+int launch_gemm(const __nv_bfloat16* sa, int64_t a_rows_pad, const __nv_bfloat16* sb, int64_t b_rows_pad,
+                int64_t k_pad, int64_t m, int64_t n, float* C, int64_t ldc, float alpha, float beta, unsigned* err,
+                cudaStream_t st) {
+    Params p;
+    std::memset(&p, 0, sizeof(p));
+    p.num_m_tiles = (int)(a_rows_pad / BM);
+    p.num_n_tiles = (int)(b_rows_pad / BN);
+    p.num_tiles = p.num_m_tiles * p.num_n_tiles;
+    p.kb_count = (int)(k_pad / BKE);
+    p.a_rows_pad = (int)a_rows_pad;
+    p.b_rows_pad = (int)b_rows_pad;
+    p.m = m; p.n = n; p.ldc = ldc;
+    p.C = C;
+    p.alpha = alpha;
+    p.beta = beta;
+    p.beta_zero = beta == 0.0f;
+    p.err = err;
+    CUtensorMap tmA, tmB;
+    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, sa, (uint64_t)k_pad, (uint64_t)(3 * a_rows_pad),
+                           (uint64_t)k_pad * 2, BKE, BM));
+    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, sb, (uint64_t)k_pad, (uint64_t)(3 * b_rows_pad),
+                           (uint64_t)k_pad * 2, BKE, BN));
+    CGB_CHECK(gemm_attr());
+    const int grid = std::min(p.num_tiles, num_sms());
+    bf16x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
+    CGB_CUDA(cudaGetLastError());
+    return COSMA_GPU_SUCCESS;
+}
+
+void launch_split3(bool kcontig, const float* X, int64_t ld, int64_t rows, int64_t k, int64_t k_pad, int64_t rows_pad,
+                   __nv_bfloat16* out, cudaStream_t st) {
+    const dim3 grid((unsigned)(rows_pad / 32), (unsigned)(k_pad / 64));
+    if (kcontig) split3_kernel<true><<<grid, 256, 0, st>>>(X, ld, rows, k, k_pad, rows_pad, out);
+    else split3_kernel<false><<<grid, 256, 0, st>>>(X, ld, rows, k, k_pad, rows_pad, out);
+}
+
 }  // namespace b3
 
 int bf16x3_sgemm(const GemmDesc& g, cudaStream_t st) {
@@ -302,46 +357,11 @@ int bf16x3_sgemm(const GemmDesc& g, cudaStream_t st) {
     auto* sb = (__nv_bfloat16*)w->slicesB.ptr;
     const float* A = (const float*)g.A;
     const float* B = (const float*)g.B;
-    {
-        dim3 gA((unsigned)(m_pad / 32), (unsigned)(k_pad / 64)), gB((unsigned)(n_pad / 32), (unsigned)(k_pad / 64));
-        if (ta) split3_kernel<true><<<gA, 256, 0, st>>>(A, g.lda, m, k, k_pad, m_pad, sa);
-        else split3_kernel<false><<<gA, 256, 0, st>>>(A, g.lda, m, k, k_pad, m_pad, sa);
-        if (!tb) split3_kernel<true><<<gB, 256, 0, st>>>(B, g.ldb, n, k, k_pad, n_pad, sb);
-        else split3_kernel<false><<<gB, 256, 0, st>>>(B, g.ldb, n, k, k_pad, n_pad, sb);
-        CGB_CUDA(cudaGetLastError());
-    }
-    Params p;
-    std::memset(&p, 0, sizeof(p));
-    p.num_m_tiles = (int)(m_pad / BM);
-    p.num_n_tiles = (int)(n_pad / BN);
-    p.num_tiles = p.num_m_tiles * p.num_n_tiles;
-    p.kb_count = (int)(k_pad / BKE);
-    p.a_rows_pad = (int)m_pad;
-    p.b_rows_pad = (int)n_pad;
-    p.m = m; p.n = n; p.ldc = g.ldc;
-    p.C = (float*)g.C;
-    p.alpha = (float)g.alpha[0];
-    p.beta = (float)g.beta[0];
-    p.beta_zero = g.beta[0] == 0.0;
-    p.err = (unsigned*)w->err.ptr;
-    CUtensorMap tmA, tmB;
-    CGB_CHECK(make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, sa, (uint64_t)k_pad, (uint64_t)(3 * m_pad),
-                           (uint64_t)k_pad * 2, BKE, BM));
-    CGB_CHECK(make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, sb, (uint64_t)k_pad, (uint64_t)(3 * n_pad),
-                           (uint64_t)k_pad * 2, BKE, BN));
-    static PerDevice<bool> attr;  // the attribute is set once per device
-    bool done = false;
-    CGB_CHECK(attr.get(
-        [](bool& v) {
-            CGB_CUDA(cudaFuncSetAttribute(bf16x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          SMEM_BYTES));
-            v = true;
-            return COSMA_GPU_SUCCESS;
-        },
-        &done));
-    const int grid = std::min(p.num_tiles, num_sms());
-    bf16x3_gemm_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(tmA, tmB, p);
+    launch_split3(ta, A, g.lda, m, k, k_pad, m_pad, sa, st);
+    launch_split3(!tb, B, g.ldb, n, k, k_pad, n_pad, sb, st);
     CGB_CUDA(cudaGetLastError());
+    CGB_CHECK(launch_gemm(sa, m_pad, sb, n_pad, k_pad, m, n, (float*)g.C, g.ldc, (float)g.alpha[0], (float)g.beta[0],
+                          (unsigned*)w->err.ptr, st));
     CGB_CUDA(cudaMemcpyAsync(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CGB_CUDA(cudaStreamSynchronize(st));
     if (*w->host_err)
@@ -349,5 +369,287 @@ int bf16x3_sgemm(const GemmDesc& g, cudaStream_t st) {
                          "bf16x3 gemm: a pipeline wait timed out (device code " + std::to_string(*w->host_err) + ")");
     return COSMA_GPU_SUCCESS;
 }
+
+namespace b3 {
+
+// ------------------------------------------------------ host operands, overlapped
+// One-step SGEMM on host A, B and C (C = alpha op(A) op(B) + beta C) with the
+// host link's copies overlapped with the work: op(A) arrives in row panels
+// and op(B) in column panels, each
+// panel's three BF16 slices are split on a second stream as it lands, block
+// (i, j)'s GEMM runs once both its panels are split, and its C block leaves
+// while later blocks compute.  Nothing is chosen from the data, so no block
+// waits for a check, and every output's K loop is the one-step call's: the
+// same bits.  The first panel of each operand is copied by the calling
+// thread (a pageable one by the device copy kernel, before any kernel of the
+// call runs), every later copy by the copy thread through the copy engines.
+constexpr int kRing = 4;            // C slots in flight
+constexpr int kMaxPanels = 8;
+constexpr int kEvents = 2 * kMaxPanels + 3 * kRing;
+
+struct PipeWS {
+    DeviceBuffer a, b, sa, sb, C[kRing], err;
+    unsigned* host_err = nullptr;
+    std::vector<cudaEvent_t> ev;
+    cudaStream_t ss = nullptr;  // the slice splits, beside the GEMMs
+    std::unique_ptr<CopyWorker> worker;
+};
+std::mutex g_pipe_mu;
+std::map<std::pair<int, cudaStream_t>, PipeWS*> g_pipe;
+
+PipeWS* pipe_ws(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_pipe_mu);
+    auto& w = g_pipe[{dev, s}];
+    if (!w) w = new PipeWS();
+    if (!w->host_err && pinned_alloc((void**)&w->host_err, sizeof(unsigned)) != cudaSuccess) w->host_err = nullptr;
+    if (w->ev.empty()) {
+        w->ev.assign(kEvents, nullptr);
+        for (auto& e : w->ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) e = nullptr;
+    }
+    if (!w->ss && cudaStreamCreateWithFlags(&w->ss, cudaStreamNonBlocking) != cudaSuccess) w->ss = nullptr;
+    if (!w->worker) {
+        try {
+            w->worker.reset(new CopyWorker(dev));
+        } catch (...) {
+            w->worker.reset();
+        }
+    }
+    cudaGetLastError();
+    return w;
+}
+
+void release_stream(cudaStream_t s) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    PipeWS* pw = nullptr;
+    Workspace* w = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_pipe_mu);
+        auto it = g_pipe.find({dev, s});
+        if (it != g_pipe.end()) {
+            pw = it->second;
+            g_pipe.erase(it);
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        auto it = g_ws.find({dev, s});
+        if (it != g_ws.end()) {
+            w = it->second;
+            g_ws.erase(it);
+        }
+    }
+    if (pw) {
+        pw->worker.reset();  // runs what is queued, then joins
+        if (pw->host_err) cudaFreeHost(pw->host_err);
+        for (auto e : pw->ev)
+            if (e) cudaEventDestroy(e);
+        if (pw->ss) {
+            cudaStreamSynchronize(pw->ss);
+            cudaStreamDestroy(pw->ss);
+        }
+        delete pw;
+    }
+    if (w) {
+        if (w->host_err) cudaFreeHost(w->host_err);
+        delete w;
+    }
+    cudaGetLastError();
+}
+
+int sgemm_host_body(const GemmDesc& g, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds, int64_t* h2d_bytes,
+                    int64_t* d2h_bytes, bool* taken) {
+    *taken = false;
+    const int64_t m = g.m, n = g.n, k = g.k;
+    if (g.scalar != Scalar::S || m < 1 || n < 1 || k < 1) return COSMA_GPU_SUCCESS;
+    if (m > (int64_t)1 << 24 || n > (int64_t)1 << 24 || k > (int64_t)64 * 65535) return COSMA_GPU_SUCCESS;
+    const bool a_kc = g.opa != 0, b_kc = g.opb == 0;  // op(A) rows / op(B) columns contiguous along K
+    // op(A) in 2 row panels and op(B) in up to 4 column panels, without a
+    // shorter lead panel: the GEMM of a 2048-row block leaves more of its
+    // last wave idle than the earlier start gains (16384^3 from pinned
+    // buffers: 34.9 ms per call against 38.6 with the lead panel).
+    const Panels PA = make_panels(m, m >= 2048 ? 2 : 1, m);
+    const Panels PB = make_panels(n, n >= 4096 ? 4 : (n >= 2048 ? 2 : 1), n);
+    const int MA = PA.count, NB = PB.count, NP = MA + NB;
+    if (MA * NB < 2 || MA > kMaxPanels / 2 || NB > kMaxPanels / 2) return COSMA_GPU_SUCCESS;
+    PipeWS* w = pipe_ws(cs);
+    if (!w->host_err || !w->ss || !w->worker) return COSMA_GPU_SUCCESS;  // the regular path
+    for (auto e : w->ev)
+        if (!e) return COSMA_GPU_SUCCESS;
+    cudaStream_t ss = w->ss;
+    CopyWorker& cw = *w->worker;
+    const int64_t k_pad = ceil_div(k, BKE) * BKE;
+    const float* A = (const float*)g.A;
+    const float* B = (const float*)g.B;
+    float* C = (float*)g.C;
+    const bool beta_zero = g.beta[0] == 0.0;
+
+    // panel geometry: compact device copies, slice stacks of 3 x rows_pad rows
+    int64_t offA[kMaxPanels], offB[kMaxPanels], soffA[kMaxPanels], soffB[kMaxPanels];
+    int64_t a_elems = 0, b_elems = 0, sa_elems = 0, sb_elems = 0;
+    for (int i = 0; i < MA; ++i) {
+        offA[i] = a_elems; a_elems += PA.rows(i, m) * k;
+        soffA[i] = sa_elems; sa_elems += 3 * ceil_div(PA.rows(i, m), BM) * BM * k_pad;
+    }
+    for (int j = 0; j < NB; ++j) {
+        offB[j] = b_elems; b_elems += PB.rows(j, n) * k;
+        soffB[j] = sb_elems; sb_elems += 3 * ceil_div(PB.rows(j, n), BN) * BN * k_pad;
+    }
+    const int NBLK = MA * NB, NR = std::min(NBLK, kRing);
+    // everything that could allocate is reserved before the first copy
+    CGB_CHECK(w->a.reserve((size_t)a_elems * 4, cs));
+    CGB_CHECK(w->b.reserve((size_t)b_elems * 4, cs));
+    CGB_CHECK(w->sa.reserve((size_t)sa_elems * 2, cs));
+    CGB_CHECK(w->sb.reserve((size_t)sb_elems * 2, cs));
+    for (int r = 0; r < NR; ++r) CGB_CHECK(w->C[r].reserve((size_t)PA.largest() * PB.largest() * 4, cs));
+    CGB_CHECK(w->err.reserve(sizeof(unsigned), cs));
+    CGB_CUDA(cudaMemsetAsync(w->err.ptr, 0, sizeof(unsigned), cs));
+    CGB_CUDA(cudaStreamSynchronize(cs));
+    float* dA = (float*)w->a.ptr;
+    float* dB = (float*)w->b.ptr;
+    auto* sa = (__nv_bfloat16*)w->sa.ptr;
+    auto* sb = (__nv_bfloat16*)w->sb.ptr;
+    int evi = 0;
+    auto next_event = [&]() { return w->ev[evi++]; };
+    cudaEvent_t ev_copy[kMaxPanels], ev_split[kMaxPanels];
+    uint64_t tk_copy[kMaxPanels] = {};
+    bool split_issued[kMaxPanels] = {};
+    *taken = true;  // from here the call owns C
+    *h2d_bytes = 0;
+    *d2h_bytes = 0;
+
+    auto copy_task = [](void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t cols,
+                        cudaMemcpyKind kind, cudaStream_t st, cudaEvent_t wait_ev, cudaEvent_t done_ev) {
+        return [=]() -> int {
+            if (wait_ev) CGB_CUDA(cudaStreamWaitEvent(st, wait_ev, 0));
+            CGB_CHECK(copy_2d_from_thread(dst, dpitch, src, spitch, width, cols, kind, st));
+            CGB_CUDA(cudaEventRecord(done_ev, st));
+            return COSMA_GPU_SUCCESS;
+        };
+    };
+    auto copy_panel = [&](int p) -> int {
+        ev_copy[p] = next_event();
+        void* dst;
+        const void* src;
+        size_t dpitch, spitch, width, cols;
+        if (p < MA) {
+            const int64_t i0 = PA.first(p), mi = PA.rows(p, m);
+            dst = dA + offA[p];
+            if (!a_kc) { dpitch = mi * 4; src = A + i0; spitch = g.lda * 4; width = mi * 4; cols = k; }
+            else { dpitch = k * 4; src = A + i0 * g.lda; spitch = g.lda * 4; width = k * 4; cols = mi; }
+            *h2d_bytes += mi * k * 4;
+        } else {
+            const int j = p - MA;
+            const int64_t j0 = PB.first(j), nj = PB.rows(j, n);
+            dst = dB + offB[j];
+            if (b_kc) { dpitch = k * 4; src = B + j0 * g.ldb; spitch = g.ldb * 4; width = k * 4; cols = nj; }
+            else { dpitch = nj * 4; src = B + j0; spitch = g.ldb * 4; width = nj * 4; cols = k; }
+            *h2d_bytes += nj * k * 4;
+        }
+        if (p == 0 || p == MA) {  // before any kernel of the call: the calling thread
+            CGB_CHECK(copy_2d_overlapped(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, hs));
+            CGB_CUDA(cudaEventRecord(ev_copy[p], hs));
+            tk_copy[p] = 0;
+        } else {
+            tk_copy[p] = cw.post(copy_task(dst, dpitch, src, spitch, width, cols, cudaMemcpyHostToDevice, hs,
+                                           nullptr, ev_copy[p]));
+        }
+        return COSMA_GPU_SUCCESS;
+    };
+    // the slices of panel p, on ss once it has landed
+    auto split_panel = [&](int p) -> int {
+        if (split_issued[p]) return COSMA_GPU_SUCCESS;
+        split_issued[p] = true;
+        CGB_CHECK(cw.wait(tk_copy[p]));  // its event is recorded
+        CGB_CUDA(cudaStreamWaitEvent(ss, ev_copy[p], 0));
+        if (p < MA) {
+            const int64_t mi = PA.rows(p, m);
+            launch_split3(a_kc, dA + offA[p], a_kc ? k : mi, mi, k, k_pad, ceil_div(mi, BM) * BM, sa + soffA[p], ss);
+        } else {
+            const int j = p - MA;
+            const int64_t nj = PB.rows(j, n);
+            launch_split3(b_kc, dB + offB[j], b_kc ? k : nj, nj, k, k_pad, ceil_div(nj, BN) * BN, sb + soffB[j], ss);
+        }
+        CGB_CUDA(cudaGetLastError());
+        ev_split[p] = next_event();
+        CGB_CUDA(cudaEventRecord(ev_split[p], ss));
+        return COSMA_GPU_SUCCESS;
+    };
+
+    // copies: the lead panels, then op(B)'s (block row 0 uses them), then op(A)'s
+    CGB_CHECK(copy_panel(0));
+    CGB_CHECK(copy_panel(MA));
+    for (int p = MA + 1; p < NP; ++p) CGB_CHECK(copy_panel(p));
+    for (int p = 1; p < MA; ++p) CGB_CHECK(copy_panel(p));
+
+    cudaEvent_t ev_gemm[kRing], ev_out[kRing], ev_cin[kRing];
+    for (int r = 0; r < NR; ++r) {
+        ev_gemm[r] = next_event();
+        ev_out[r] = next_event();
+        ev_cin[r] = next_event();
+    }
+    bool out_used[kRing] = {};
+    uint64_t tk_out[kRing] = {};
+    const float alpha = (float)g.alpha[0], beta = (float)g.beta[0];
+    for (int b = 0; b < NBLK; ++b) {
+        const int i = b / NB, j = b % NB, slot = b % NR;
+        const int64_t i0 = PA.first(i), mi = PA.rows(i, m), j0 = PB.first(j), nj = PB.rows(j, n);
+        CGB_CHECK(split_panel(i));
+        CGB_CHECK(split_panel(MA + j));
+        CGB_CUDA(cudaStreamWaitEvent(cs, ev_split[i], 0));
+        CGB_CUDA(cudaStreamWaitEvent(cs, ev_split[MA + j], 0));
+        float* cdev = (float*)w->C[slot].ptr;
+        float* chost = C + i0 + j0 * g.ldc;
+        if (!beta_zero) {  // the old C block comes in once its slot has been drained
+            const uint64_t t = cw.post(copy_task(cdev, mi * 4, chost, g.ldc * 4, mi * 4, nj, cudaMemcpyHostToDevice,
+                                                 hs, out_used[slot] ? ev_out[slot] : nullptr, ev_cin[slot]));
+            *h2d_bytes += mi * nj * 4;
+            CGB_CHECK(cw.wait(t));
+            CGB_CUDA(cudaStreamWaitEvent(cs, ev_cin[slot], 0));
+        } else if (out_used[slot]) {
+            CGB_CHECK(cw.wait(tk_out[slot]));
+            CGB_CUDA(cudaStreamWaitEvent(cs, ev_out[slot], 0));
+        }
+        const int64_t mi_pad = ceil_div(mi, BM) * BM, nj_pad = ceil_div(nj, BN) * BN;
+        CGB_CHECK(launch_gemm(sa + soffA[i], mi_pad, sb + soffB[j], nj_pad, k_pad, mi, nj, cdev, mi, alpha, beta,
+                              (unsigned*)w->err.ptr, cs));
+        CGB_CUDA(cudaEventRecord(ev_gemm[slot], cs));
+        tk_out[slot] = cw.post(copy_task(chost, g.ldc * 4, cdev, mi * 4, mi * 4, nj, cudaMemcpyDeviceToHost, ds,
+                                         ev_gemm[slot], ev_out[slot]));
+        *d2h_bytes += mi * nj * 4;
+        out_used[slot] = true;
+    }
+    CGB_CHECK(cw.drain());
+    for (cudaStream_t s : {cs, hs, ds, ss}) CGB_CUDA(cudaStreamSynchronize(s));
+    CGB_CUDA(cudaMemcpy(w->host_err, w->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (*w->host_err)
+        return set_error(COSMA_GPU_ERROR_DEVICE_TIMEOUT,
+                         "bf16x3 gemm: a pipeline wait timed out (device code " + std::to_string(*w->host_err) + ")");
+    return COSMA_GPU_SUCCESS;
+}
+
+}  // namespace b3
+
+int bf16x3_sgemm_host(const GemmDesc& g, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds, int64_t* h2d_bytes,
+                      int64_t* d2h_bytes, bool* taken) {
+    const int st = b3::sgemm_host_body(g, cs, hs, ds, h2d_bytes, d2h_bytes, taken);
+    if (st != COSMA_GPU_SUCCESS) {  // nothing left in flight
+        b3::PipeWS* w = b3::pipe_ws(cs);
+        if (w->worker) w->worker->drain();
+        for (cudaStream_t s : {cs, hs, ds, w->ss})
+            if (s) cudaStreamSynchronize(s);
+        cudaGetLastError();
+        if (st == COSMA_GPU_ERROR_OUT_OF_MEMORY && !*taken) {
+            for (DeviceBuffer* b : {&w->a, &w->b, &w->sa, &w->sb}) b->release();
+            for (auto& c : w->C) c.release();
+        }
+    }
+    return st;
+}
+
+void bf16x3_release_stream(cudaStream_t s) { b3::release_stream(s); }
 
 }  // namespace cgb

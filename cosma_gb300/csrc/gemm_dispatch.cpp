@@ -136,6 +136,7 @@ int cosma_gpu_release_workspaces(void* stream) {
     cgb::clear_error();
     cgb::ozaki_release_stream((cudaStream_t)stream);
     cgb::ozaki2_release_stream((cudaStream_t)stream);
+    cgb::bf16x3_release_stream((cudaStream_t)stream);
     return COSMA_GPU_SUCCESS;
 }
 

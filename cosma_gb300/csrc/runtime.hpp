@@ -151,6 +151,12 @@ void ozaki2_release_stream(cudaStream_t s);
 // scalars do not pipeline, or when the first panels' modulus count differs
 // from the whole data's or the data holds Inf/NaN: the caller then runs the
 // regular path.
+// One-step 3xBF16 SGEMM on host A, B, C with the host copies overlapped with
+// the slice splits and block GEMMs (bf16x3.cu); *taken = false (nothing done)
+// when the shape does not pipeline.
+int bf16x3_sgemm_host(const GemmDesc& g, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds, int64_t* h2d_bytes,
+                      int64_t* d2h_bytes, bool* taken);
+void bf16x3_release_stream(cudaStream_t s);
 int ozaki2_gemm_host(const GemmDesc& g, int moduli, cudaStream_t cs, cudaStream_t hs, cudaStream_t ds,
                       cosma_gpu_ozaki_info* info, int64_t* h2d_bytes, int64_t* d2h_bytes, bool* taken);
 

@@ -45,6 +45,7 @@ struct cosma_gpu_mm_handle {
     std::mutex mu;
     cosma_gpu_ozaki_info last_info{0, 0, 0, 0, 0.0, 0.0, 0.0};
     int64_t last_h2d_bytes = 0, last_d2h_bytes = 0;
+    int last_overlapped = 0;  // the last call ran in an overlapped one-step form
     cudaEvent_t ev_ready[2] = {}, ev_free[2] = {}, ev_cin[2] = {}, ev_cdone[2] = {}, ev_cout[2] = {};
 };
 
@@ -171,6 +172,7 @@ int tmm_gemm(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int64_t m, int
     const bool trivial = (k == 0) || is_zero(alpha, sc);
     cosma_gpu_ozaki_info* info = &h->last_info;
     *info = cosma_gpu_ozaki_info{0, 0, 0, 0, 0.0, 0.0, 0.0, 0, 0};
+    h->last_overlapped = 0;
 
     if (trivial && is_one(beta, sc)) return COSMA_GPU_SUCCESS;  // C unchanged
     if (dC && (trivial || (dA && dB))) {  // everything already in HBM
@@ -258,6 +260,30 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
             h->last_h2d_bytes = h2d;
             h->last_d2h_bytes = d2h;
             h->last_device_c = nullptr;
+            h->last_overlapped = 1;
+            return COSMA_GPU_SUCCESS;
+        }
+    }
+    // One step on host operands with 3xBF16 (float under the AUTO or BF16X3
+    // method): the same overlapped form around the slice splits and block
+    // GEMMs (16384^3 from pinned buffers: 34.9 to 35.6 ms per call against 44
+    // ms with the copies before and after the GEMM).
+    const bool b3 = sc == Scalar::S && (h->method == COSMA_GPU_METHOD_AUTO || h->method == COSMA_GPU_METHOD_BF16X3);
+    if (b3 && env_bool("COSMA_GPU_BF16X3_OVERLAP", true) && !dA && !dB && !dC && !trivial && !keep_on_device &&
+        nsteps == 1 && h->streams.size() >= 2) {
+        const GemmDesc g = make_gemm_desc(sc, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        int64_t h2d = 0, d2h = 0;
+        bool taken = false;
+        const size_t S = h->streams.size();
+        const int st = bf16x3_sgemm_host(g, h->streams[0], h->streams[1], h->streams[std::min<size_t>(2, S - 1)],
+                                         &h2d, &d2h, &taken);
+        if (st != COSMA_GPU_SUCCESS && (taken || st != COSMA_GPU_ERROR_OUT_OF_MEMORY)) return st;
+        if (st != COSMA_GPU_SUCCESS) clear_error();
+        if (taken && st == COSMA_GPU_SUCCESS) {
+            h->last_h2d_bytes = h2d;
+            h->last_d2h_bytes = d2h;
+            h->last_device_c = nullptr;
+            h->last_overlapped = 1;
             return COSMA_GPU_SUCCESS;
         }
     }
@@ -284,6 +310,7 @@ int tmm_stream_tiles(cosma_gpu_mm_handle* h, Scalar sc, char ta, char tb, int op
     cudaEvent_t* ev_cout = h->ev_cout;      // C slot drained to its destination
     bool slot_used[R] = {false, false}, cslot_used[R] = {false, false};
     h->last_h2d_bytes = 0;
+    h->last_overlapped = 0;
     h->last_d2h_bytes = 0;
     const double one[2] = {1.0, 0.0};
     const bool beta_zero = is_zero(beta, sc);
@@ -460,6 +487,7 @@ void cosma_gpu_tmm_destroy_context(cosma_gpu_mm_handle* h) {
         for (auto s : h->streams) {
             cgb::ozaki_release_stream(s);
             cgb::ozaki2_release_stream(s);
+            cgb::bf16x3_release_stream(s);
             cudaStreamDestroy(s);
         }
         for (int i = 0; i < 2; ++i)
@@ -549,6 +577,8 @@ int cosma_gpu_tmm_tiles(cosma_gpu_mm_handle* h, int* tile_m, int* tile_n, int* t
 }
 
 void* cosma_gpu_tmm_device_buffer_c(cosma_gpu_mm_handle* h) { return h ? h->last_device_c : nullptr; }
+
+int cosma_gpu_tmm_last_overlapped(cosma_gpu_mm_handle* h) { return h ? h->last_overlapped : 0; }
 
 int cosma_gpu_tmm_last_transfer_bytes(cosma_gpu_mm_handle* h, int64_t* h2d_bytes, int64_t* d2h_bytes) {
     if (!h || !h2d_bytes || !d2h_bytes)

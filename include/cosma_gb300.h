@@ -96,6 +96,12 @@ int cosma_gpu_tmm_set_method(cosma_gpu_mm_handle* handle, int method, int ozaki_
 /* Device buffer holding the C of the last call made with copy_c_back == 0
  * (replaces mm_handle::get_full_device_buffer_c(), src/cosma/gpu/nccl_utils.cpp:200). */
 void* cosma_gpu_tmm_device_buffer_c(cosma_gpu_mm_handle* handle);
+
+/* 1 when the handle's last gemm call ran in an overlapped one-step form
+ * (host A, B and C in one step: the Chinese-remainder method for double and
+ * real-scaled complex, 3xBF16 for float), else 0.
+ * New: a diagnostic of this library; the reference has no counterpart. */
+int cosma_gpu_tmm_last_overlapped(cosma_gpu_mm_handle* h);
 /* Bytes the handle's last gemm call moved host->device and device->host
  * (zero for operands that were already in device memory). */
 int cosma_gpu_tmm_last_transfer_bytes(cosma_gpu_mm_handle* handle, int64_t* h2d_bytes,

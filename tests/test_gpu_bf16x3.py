@@ -65,3 +65,49 @@ def test_bf16x3_k_zero_and_alpha_zero(native_lib, cuda):
     d1 = to_dev(np.ones((m, 1), dtype=np.float32))
     gemm_device("N", "N", m, n, 0, 1.0, d1, m, d1, 1, 2.0, dC, m, method="bf16x3", scalar="s")
     np.testing.assert_array_equal(from_dev(dC, m, n), 2.0 * C0)
+
+
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+@pytest.mark.parametrize("ta,tb,beta,shape", [("N", "N", 0.0, (2100, 2300, 300)), ("T", "N", -0.5, (2100, 2300, 300)),
+                                              ("N", "T", 1.0, (4500, 4200, 64)), ("T", "T", 0.0, (1000, 4500, 70))])
+def test_bf16x3_overlapped_one_step(native_lib, cuda, monkeypatch, ta, tb, beta, shape, pinned):
+    """SGEMM (3xBF16, the AUTO method for float) through the Tiled-MM entry on
+    host arrays in the overlapped one-step form: panels split as they land,
+    block GEMMs, C blocks copied out while later ones compute.  The bits of
+    the same call without overlap and of the device call; transfers count
+    A, B (and C when read) once."""
+    import torch
+    from cosma_gb300 import gemm, gemm_device, make_context
+    m, n, k = shape
+    ldc = m + 1
+    A = oracle.normal(_op_shape(ta, m, k), 31, dtype=np.float32)
+    B = oracle.normal(_op_shape(tb, k, n), 32, dtype=np.float32)
+    C0 = np.zeros((ldc, n), dtype=np.float32)
+    C0[:m] = oracle.normal((m, n), 33, dtype=np.float32)
+
+    def host(X):
+        if not pinned:
+            return np.asfortranarray(X.copy()), None
+        t = torch.from_numpy(np.ascontiguousarray(X.T).reshape(-1)).pin_memory()
+        return t, t
+
+    outs = {}
+    for mode in ("ON", "OFF"):
+        monkeypatch.setenv("COSMA_GPU_BF16X3_OVERLAP", mode)
+        hA, _ = host(A)
+        hB, _ = host(B)
+        hC, tC = host(C0)
+        h = make_context("s", 3)
+        gemm(h, ta, tb, m, n, k, 1.25, hA, A.shape[0], hB, B.shape[0], beta, hC, ldc)
+        outs[mode] = (np.array(tC.numpy().reshape(n, ldc).T if tC is not None else hC), h.last_overlapped(),
+                      h.transfer_bytes())
+        h.close()
+    on, ov_on, moved = outs["ON"]
+    off, ov_off, _ = outs["OFF"]
+    assert ov_on and not ov_off
+    assert on.tobytes() == off.tobytes()
+    np.testing.assert_array_equal(on[m:], C0[m:])  # rows past m untouched
+    assert moved == (4 * (m * k + k * n + (m * n if beta != 0 else 0)), 4 * m * n)
+    dA, dB, dC = to_dev(A), to_dev(B), to_dev(C0, ldc)
+    gemm_device(ta, tb, m, n, k, 1.25, dA, A.shape[0], dB, B.shape[0], beta, dC, ldc, method="bf16x3")
+    assert on[:m].tobytes() == np.ascontiguousarray(from_dev(dC, m, n, ldc)).tobytes()
